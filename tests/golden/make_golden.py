@@ -1,0 +1,186 @@
+"""Generate the golden fixtures in this directory by running the UNMODIFIED
+ceviche 0.1.3 reference (forward code only) through the forward-only
+autograd/matplotlib stand-in in ``refshim/``.
+
+Usage (needs a checkout of the reference; not run by the test suite):
+    python tests/golden/make_golden.py /path/to/ceviche-checkout
+
+Fixtures (all small, seeded):
+    stencil_ops.npz     A@x and A^T@x of the assembled Ez/Hz system matrices
+                        (fdfd.py:172-233 via _make_A + utils.make_sparse)
+    fdfd_fields.npz     fdfd_ez / fdfd_hz .solve outputs (fdfd.py:58-76)
+    fdtd_fields.npz     fdtd.forward fields after TM and TE runs (fdtd.py:74-144)
+    grad_fd.npz         central finite differences of reference objectives
+                        (gradient pins for the FDFD and FDTD adjoints)
+"""
+import os
+import sys
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def load_reference(ref_root):
+    sys.path.insert(0, os.path.join(HERE, "refshim"))
+    sys.path.insert(0, ref_root)
+    warnings.simplefilter("ignore")
+    import ceviche  # noqa: E402
+    from ceviche import utils, constants  # noqa: E402
+    return ceviche, utils, constants
+
+
+def system_matrix(F, eps, utils):
+    entries, indices = F._make_A(eps.ravel())
+    return utils.make_sparse(entries, indices, shape=(F.N, F.N))
+
+
+def stencil_cases():
+    # (Nx, Ny, npml, bloch, omega_scale, dL)
+    return [
+        (37, 29, [5, 4], (0.3, -0.7), 1.0, 25e-9),
+        (16, 12, [3, 0], None, 1.3, 40e-9),
+        (30, 30, [10, 10], None, 1.0, 1e-6),
+        (9, 7, [0, 0], (1.1, 0.0), 0.8, 50e-9),
+    ]
+    # 1D grids (Nx or Ny == 1) are left out: the reference's own solve fails
+    # there (utils.get_entries_indices on a dia-format derivative matrix).
+
+
+def main(ref_root):
+    ceviche, utils, constants = load_reference(ref_root)
+    C_0 = constants.C_0
+    rng = np.random.default_rng(20261203)
+    out = {}
+
+    # ---------------------------------------------------------------- operators
+    for k, (Nx, Ny, npml, bloch, osc, dL) in enumerate(stencil_cases()):
+        omega = osc * 2 * np.pi * C_0 / 1.55e-6
+        if dL == 1e-6:
+            omega = 2 * np.pi * 200e12
+        eps = rng.uniform(1.0, 12.25, size=(Nx, Ny))
+        x = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+        for pol, cls in (("ez", ceviche.fdfd_ez), ("hz", ceviche.fdfd_hz)):
+            F = cls(omega, dL, eps, npml, bloch_phases=bloch)
+            A = system_matrix(F, eps, utils)
+            out[f"c{k}_{pol}_Ax"] = A.dot(x)
+            out[f"c{k}_{pol}_ATx"] = A.T.dot(x)
+        out[f"c{k}_eps"] = eps
+        out[f"c{k}_x"] = x
+        out[f"c{k}_meta"] = np.array([Nx, Ny, npml[0], npml[1],
+                                      0.0 if bloch is None else bloch[0],
+                                      0.0 if bloch is None else bloch[1], omega, dL])
+    np.savez_compressed(os.path.join(HERE, "stencil_ops.npz"), **out)
+
+    # ------------------------------------------------------------------ fields
+    out = {}
+    cases = [
+        ("t30", 30, 30, [10, 10], None, 2 * np.pi * 200e12, 1e-6, 1.0, 2.0),
+        ("w60", 60, 48, [8, 6], (0.4, 0.0), 2 * np.pi * C_0 / 1.55e-6, 25e-9, 1.0, 12.25),
+    ]
+    for name, Nx, Ny, npml, bloch, omega, dL, lo, hi in cases:
+        eps = rng.uniform(lo, hi, size=(Nx, Ny))
+        src = np.zeros((Nx, Ny))
+        src[Nx // 2, Ny // 2] = 1.0
+        src[npml[0] + 2, Ny // 3:Ny // 3 + 4] = 0.5
+        Fe = ceviche.fdfd_ez(omega, dL, eps, npml, bloch_phases=bloch)
+        Fh = ceviche.fdfd_hz(omega, dL, eps, npml, bloch_phases=bloch)
+        out[f"{name}_eps"] = eps
+        out[f"{name}_src"] = src
+        out[f"{name}_meta"] = np.array([npml[0], npml[1], 0.0 if bloch is None else bloch[0],
+                                        0.0 if bloch is None else bloch[1], omega, dL])
+        out[f"{name}_ez"] = np.stack(Fe.solve(src))
+        out[f"{name}_hz"] = np.stack(Fh.solve(src))
+    np.savez_compressed(os.path.join(HERE, "fdfd_fields.npz"), **out)
+
+    # -------------------------------------------------------------------- FDTD
+    out = {}
+    Nx, Ny, npml, dL = 24, 20, [4, 3, 0], 25e-9
+    eps = rng.uniform(1.0, 6.0, size=(Nx, Ny))
+    F = ceviche.fdtd(eps[:, :, None], dL, npml)
+    prof = np.zeros((Nx, Ny, 1))
+    prof[11, 9, 0] = 1.0
+    prof[6, 14, 0] = -0.4
+    steps, t0, sg = 300, 60, 15
+    amps = np.exp(-(np.arange(steps) - t0) ** 2 / 2 / sg ** 2) * np.cos(0.3 * np.arange(steps))
+    snaps = []
+    for t in range(steps):
+        f = F.forward(Jz=prof * amps[t])
+        if (t + 1) % 50 == 0:
+            snaps.append(f["Ez"][:, :, 0].copy())
+    out["tm_eps"], out["tm_prof"], out["tm_amps"] = eps, prof[:, :, 0], amps
+    out["tm_meta"] = np.array([npml[0], npml[1], dL, F.dt])
+    out["tm_Ez_snaps"] = np.stack(snaps)
+    for k in ("Hx", "Hy", "Dz", "Ez", "Ex", "Ey", "Hz"):
+        out[f"tm_final_{k}"] = f[k][:, :, 0].copy()
+    # TE run (Jx, Jy sources) plus a simultaneous Jz
+    F = ceviche.fdtd(eps[:, :, None], dL, npml)
+    for t in range(200):
+        f = F.forward(Jx=prof * amps[t], Jy=-0.5 * prof * amps[t], Jz=0.25 * prof * amps[t])
+    for k in ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Hx", "Hy", "Hz"):
+        out[f"te_final_{k}"] = f[k][:, :, 0].copy()
+    np.savez_compressed(os.path.join(HERE, "fdtd_fields.npz"), **out)
+
+    # ------------------------------------------------------- gradient pins (FD)
+    out = {}
+    # FDFD, the reference gradient-test geometry (test_gradients_fdfd.py:34-59),
+    # seeded eps, objective J = sum|Fz|^2 + |Fx|^2 + |Fy|^2, source = eps*point
+    Nx = Ny = 30
+    omega, dL, npml = 2 * np.pi * 200e12, 1e-6, [10, 10]
+    eps0 = rng.random((Nx, Ny)) + 1
+    src = np.zeros((Nx, Ny))
+    src[15, 15] = 1.0
+    pix = rng.choice(Nx * Ny, size=12, replace=False)
+    pix = np.unique(np.concatenate([pix, [15 * Ny + 15, 14 * Ny + 15, 15 * Ny + 16]]))
+    h = 1e-5
+    for pol, cls in (("ez", ceviche.fdfd_ez), ("hz", ceviche.fdfd_hz)):
+        Fo = cls(omega, dL, eps0, npml)
+
+        def J(e):
+            Fo.eps_r = e
+            a, b, c = Fo.solve(e * src)
+            return np.sum(np.abs(a) ** 2) + np.sum(np.abs(b) ** 2) + np.sum(np.abs(c) ** 2)
+
+        g = []
+        for p in pix:
+            ep, em = eps0.copy(), eps0.copy()
+            ep.flat[p] += h
+            em.flat[p] -= h
+            g.append((J(ep) - J(em)) / (2 * h))
+        out[f"fdfd_{pol}_grad"] = np.array(g)
+        out[f"fdfd_{pol}_J"] = np.array(J(eps0))
+    out["fdfd_eps"], out["fdfd_src"], out["fdfd_pix"] = eps0, src, pix
+
+    # FDTD, the reference gradient-test geometry (test_gradients_fdtd.py:28-50)
+    Nx = Ny = 8
+    dL, npml = 5e-8, [2, 2, 0]
+    steps, t0, sg = 500, 300, 20
+    eps0 = rng.random((Nx, Ny)) + 1
+    prof = np.zeros((Nx, Ny, 1))
+    prof[Nx // 2, Ny // 2, 0] = 1.0
+    amps = np.exp(-(np.arange(steps) - t0) ** 2 / 2 / sg ** 2)
+
+    def S(e):
+        Fd = ceviche.fdtd(e[:, :, None], dL, npml)
+        s = 0.0
+        for t in range(steps):
+            f = Fd.forward(Jz=prof * amps[t])
+            s += np.sum(f["Ex"] + f["Ey"] + f["Ez"])
+        return s
+
+    h = 1e-4
+    g = np.zeros(Nx * Ny)
+    for p in range(Nx * Ny):
+        ep, em = eps0.copy(), eps0.copy()
+        ep.flat[p] += h
+        em.flat[p] -= h
+        g[p] = (S(ep) - S(em)) / (2 * h)
+    out["fdtd_eps"], out["fdtd_prof"], out["fdtd_amps"] = eps0, prof[:, :, 0], amps
+    out["fdtd_grad"], out["fdtd_S"] = g, np.array(S(eps0))
+    np.savez_compressed(os.path.join(HERE, "grad_fd.npz"), **out)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CEVICHE_REF", ""))

@@ -1,0 +1,92 @@
+"""Pins the CPU oracle to fixtures produced by the unmodified reference
+(tests/golden/make_golden.py).  CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import fdfd as ofd
+from oracle import fdtd as oft
+from tests.conftest import GOLDEN
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+def _rel(a, b):
+    return np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300)
+
+
+@pytest.mark.parametrize("k", range(4))
+@pytest.mark.parametrize("pol", ["ez", "hz"])
+def test_operator_matches_reference(k, pol):
+    d = _load("stencil_ops.npz")
+    Nx, Ny, px, py, bx, by, omega, dL = d[f"c{k}_meta"]
+    A = ofd.make_A(pol, omega, dL, d[f"c{k}_eps"], [int(px), int(py)], (bx, by))
+    x = d[f"c{k}_x"]
+    assert _rel(A.dot(x), d[f"c{k}_{pol}_Ax"]) < 1e-13
+    assert _rel(A.T.dot(x), d[f"c{k}_{pol}_ATx"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", ["t30", "w60"])
+def test_fields_match_reference(name):
+    d = _load("fdfd_fields.npz")
+    px, py, bx, by, omega, dL = d[f"{name}_meta"]
+    eps, src = d[f"{name}_eps"], d[f"{name}_src"]
+    ez = ofd.solve_ez(omega, dL, eps, [int(px), int(py)], src, (bx, by))
+    hz = ofd.solve_hz(omega, dL, eps, [int(px), int(py)], src, (bx, by))
+    for got, ref in zip(ez, d[f"{name}_ez"]):
+        assert _rel(got, ref) < 1e-10
+    for got, ref in zip(hz, d[f"{name}_hz"]):
+        assert _rel(got, ref) < 1e-10
+
+
+def test_fdtd_tm_matches_reference():
+    d = _load("fdtd_fields.npz")
+    px, py, dL, dt = d["tm_meta"]
+    assert oft.time_step(dL) == dt
+    F, snaps = oft.run_tm(d["tm_eps"], dL, [int(px), int(py), 0], d["tm_prof"], d["tm_amps"],
+                          record_every=50)
+    for s, r in zip(snaps, d["tm_Ez_snaps"]):
+        assert _rel(s, r) < 1e-12
+    for k in ("Hx", "Hy", "Dz", "Ez", "Ex", "Ey", "Hz"):
+        ref = d[f"tm_final_{k}"]
+        if np.all(ref == 0):
+            assert np.all(F.f[k] == 0)
+        else:
+            assert _rel(F.f[k], ref) < 1e-12
+
+
+def test_fdtd_te_matches_reference():
+    d = _load("fdtd_fields.npz")
+    px, py, dL, dt = d["tm_meta"]
+    F = oft.FDTD2D(d["tm_eps"], dL, [int(px), int(py), 0])
+    p, a = d["tm_prof"], d["tm_amps"]
+    for t in range(200):
+        F.forward(Jx=p * a[t], Jy=-0.5 * p * a[t], Jz=0.25 * p * a[t])
+    for k in oft.FDTD2D.FIELDS:
+        assert _rel(F.f[k], d[f"te_final_{k}"]) < 1e-12, k
+
+
+@pytest.mark.parametrize("pol", ["ez", "hz"])
+def test_fdfd_adjoint_matches_reference_fd(pol):
+    """Restated reverse-mode gradient vs central differences of the reference."""
+    d = _load("grad_fd.npz")
+    eps, src, pix = d["fdfd_eps"], d["fdfd_src"], d["fdfd_pix"]
+    omega, dL, npml = 2 * np.pi * 200e12, 1e-6, [10, 10]
+    solve = ofd.solve_ez if pol == "ez" else ofd.solve_hz
+    f = solve(omega, dL, eps, npml, eps * src)
+    # J = sum |f|^2 over the three components -> torch cotangent g = 2 f
+    g = [2 * c for c in f]
+    gradf = ofd.grad_eps_ez if pol == "ez" else ofd.grad_eps_hz
+    grad = gradf(omega, dL, eps, npml, src, *g, source_times_eps=True)
+    ref = d[f"fdfd_{pol}_grad"]
+    assert _rel(grad.ravel()[pix], ref) < 1e-8
+
+
+def test_fdtd_adjoint_matches_reference_fd():
+    d = _load("grad_fd.npz")
+    eps, prof, amps = d["fdtd_eps"], d["fdtd_prof"], d["fdtd_amps"]
+    grad = oft.adjoint_tm(eps, 5e-8, [2, 2, 0], prof, amps, np.ones_like(eps), np.ones(len(amps)))
+    assert _rel(grad.ravel(), d["fdtd_grad"]) < 1e-6
