@@ -1,0 +1,829 @@
+// 2D Yee FDTD with ceviche's integrated-sigma PML, forward and adjoint.
+//
+// Update form (TM; Nz = 1, sigma_z = 0).  With a = sigma*dt/(2 eps0) on the
+// H and D sub-grids and S = C0 dt / dL, the coefficients of
+// ceviche/fdtd.py:265-316 become
+//   mHx1 = (1-aHy)/(1+aHy),  mHx2*CEx = -S/(1+aHy) dEy,
+//   mHx3*ICEx = -S/(1+aHy) (2 aHx) sum(dEy)          (same for y with x<->y)
+//   mDz0*dt = (1+aDx)(1+aDy), mDz1 = (1-aDx-aDy-aDx aDy)/((1+aDx)(1+aDy)),
+//   mDz2*CHz = S/((1+aDx)(1+aDy)) CH',  mDz4 = -4 aDx aDy/((1+aDx)(1+aDy))
+// with dEy = Ez[i,j+1]-Ez, dEx' = -(Ez[i+1,j]-Ez), CH' = (Hy-Hy[i-1])-(Hx-Hx[i,j-1])
+// (the curls of ceviche/derivatives.py:26-40 without the 1/dL factor, which
+// sits in S).  mHx4, mHy4 and mDz3 carry sigma_z and are exactly zero, so the
+// IHx, IHy and ICHz integrals never reach a field.  The PML integrals are
+// accumulated only where their coefficient is non-zero; elsewhere they are
+// multiplied by an exact zero in the reference.
+// TE (Hz, Dx, Dy) is the dual: mHz has the (1+aHx)(1+aHy) form and
+// Dx, Dy the single-axis form.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cev {
+
+constexpr double F_EPSILON_0 = 8.85418782e-12;
+constexpr double F_MU_0 = 1.25663706e-6;
+
+template <typename R>
+struct AxisCoef {
+  R aH, f1H, f2H, pH;  // H sub-grid: a, (1-a)/(1+a), S/(1+a), 1/(1+a)
+  R aD, f1D, f2D, pD;  // D sub-grid
+};
+
+}  // namespace cev
+
+struct cev_fdtd_plan_s {
+  int nx = 0, ny = 0, npml_x = 0, npml_y = 0, prec = 0;
+  double dL = 0, dt = 0, S = 0;
+  void* ax = nullptr;   // AxisCoef<R>[nx]
+  void* ay = nullptr;   // AxisCoef<R>[ny]
+  void* iez = nullptr;  // 1/eps_zz, 1/eps_xx, 1/eps_yy (R[N])
+  void* iexx = nullptr;
+  void* ieyy = nullptr;
+  void* shadow = nullptr;  // second TM state for the time-blocked run (6 N R)
+  std::vector<double> aHx, aDx, aHy, aDy;
+  size_t n() const { return (size_t)nx * ny; }
+  size_t rs() const { return prec == CEV_PREC_C128 ? sizeof(double) : sizeof(float); }
+};
+
+namespace cev {
+
+// ceviche/fdtd.py:213-222
+static double fdtd_dt(double dL) {
+  const double C_0 = 1.0 / std::sqrt(F_EPSILON_0 * F_MU_0);
+  const double dL_sum = 3.0 / (dL * dL);
+  const double dL_avg = 1.0 / std::sqrt(dL_sum);
+  return dL_avg / C_0 * 0.5;
+}
+
+// sigma on the 2X grid (ceviche/fdtd.py:224-263), returned as a = sigma dt/(2 eps0)
+static void sigma_profile(int N, int npml, double dt, std::vector<double>& aH,
+                          std::vector<double>& aD) {
+  std::vector<double> s2(2 * (size_t)N, 0.0);
+  for (int k = 0; k < 2 * npml; ++k) {
+    const int k1 = 2 * npml - k + 1;
+    const int k2 = 2 * N - 2 * npml + k;
+    const double v = (0.5 * F_EPSILON_0 / dt) * std::pow((double)k / 2 / npml, 3);
+    if (k1 >= 0 && k1 < 2 * N) s2[k1] = v;
+    if (k2 >= 0 && k2 < 2 * N) s2[k2] = v;
+  }
+  aH.resize(N);
+  aD.resize(N);
+  for (int i = 0; i < N; ++i) {
+    aH[i] = s2[2 * i + 1] * dt / (2 * F_EPSILON_0);  // sigH = sig2[1::2]
+    aD[i] = s2[2 * i] * dt / (2 * F_EPSILON_0);      // sigD = sig2[::2]
+  }
+}
+
+template <typename R>
+static std::vector<AxisCoef<R>> axis_coefs(const std::vector<double>& aH,
+                                           const std::vector<double>& aD, double S) {
+  std::vector<AxisCoef<R>> c(aH.size());
+  for (size_t i = 0; i < aH.size(); ++i) {
+    const double h = aH[i], d = aD[i];
+    c[i].aH = (R)h;
+    c[i].f1H = (R)((1 - h) / (1 + h));
+    c[i].f2H = (R)(S / (1 + h));
+    c[i].pH = (R)(1 / (1 + h));
+    c[i].aD = (R)d;
+    c[i].f1D = (R)((1 - d) / (1 + d));
+    c[i].f2D = (R)(S / (1 + d));
+    c[i].pD = (R)(1 / (1 + d));
+  }
+  return c;
+}
+
+template <typename R>
+__global__ void k_inv_eps(const double* eps, R* iez, R* iexx, R* ieyy, int nx, int ny) {
+  const size_t N = (size_t)nx * ny;
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < N;
+       n += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(n / ny), j = (int)(n % ny);
+    const double e = eps[n];
+    // ceviche/utils.py:153-176: xx averages with roll(+1) along axis 0, yy along axis 1
+    const double exx = (e + eps[(size_t)((i + nx - 1) % nx) * ny + j]) / 2;
+    const double eyy = (e + eps[(size_t)i * ny + (j + ny - 1) % ny]) / 2;
+    const double ezz = (e + e) / 2;
+    iez[n] = (R)(1.0 / ezz);
+    iexx[n] = (R)(1.0 / exx);
+    ieyy[n] = (R)(1.0 / eyy);
+  }
+}
+
+// ------------------------------------------------------------ per-step TM
+template <typename R>
+struct TMArgs {
+  int nx, ny;
+  R* hx; R* hy; R* dz; R* icex; R* icey; R* idz;
+  const R* iez;
+  const AxisCoef<R>* ax;
+  const AxisCoef<R>* ay;
+  R S;
+  const R* jz;
+};
+
+template <typename R>
+__global__ void k_tm_h(TMArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int ip = i + 1 == a.nx ? 0 : i + 1, jp = j + 1 == a.ny ? 0 : j + 1;
+  const R ez = a.dz[n] * a.iez[n];
+  const size_t nr = (size_t)i * a.ny + jp, nd = (size_t)ip * a.ny + j;
+  const R ezr = a.dz[nr] * a.iez[nr];
+  const R ezd = a.dz[nd] * a.iez[nd];
+  const R dEy = ezr - ez;
+  const R dEx = -(ezd - ez);
+  const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
+  R icx = R(0), icy = R(0);
+  if (cx.aH != R(0)) { icx = a.icex[n] + dEy; a.icex[n] = icx; }
+  if (cy.aH != R(0)) { icy = a.icey[n] + dEx; a.icey[n] = icy; }
+  a.hx[n] = cy.f1H * a.hx[n] - cy.f2H * (dEy + R(2) * cx.aH * icx);
+  a.hy[n] = cx.f1H * a.hy[n] - cx.f2H * (dEx + R(2) * cy.aH * icy);
+}
+
+template <typename R>
+__device__ __forceinline__ void dz_coefs(const AxisCoef<R>& cx, const AxisCoef<R>& cy, R S, R& m1,
+                                         R& m2, R& m4) {
+  const R ax = cx.aD, ay = cy.aD;
+  const R pd = cx.pD * cy.pD;
+  m1 = (R(1) - ax - ay - ax * ay) * pd;
+  m2 = S * pd;
+  m4 = R(-4) * ax * ay * pd;
+}
+
+template <typename R>
+__global__ void k_tm_d(TMArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int im = i == 0 ? a.nx - 1 : i - 1, jm = j == 0 ? a.ny - 1 : j - 1;
+  const R hy = a.hy[n], hx = a.hx[n];
+  const R ch = (hy - a.hy[(size_t)im * a.ny + j]) - (hx - a.hx[(size_t)i * a.ny + jm]);
+  const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
+  R m1, m2, m4;
+  dz_coefs(cx, cy, a.S, m1, m2, m4);
+  const R dz = a.dz[n];
+  R id = R(0);
+  if (m4 != R(0)) { id = a.idz[n] + dz; a.idz[n] = id; }
+  R v = m1 * dz + m2 * ch + m4 * id;
+  if (a.jz) v += a.jz[n];
+  a.dz[n] = v;
+}
+
+// ------------------------------------------------------------ per-step TE
+template <typename R>
+struct TEArgs {
+  int nx, ny;
+  R* hz; R* dx; R* dy; R* ihz; R* ichx; R* ichy;
+  const R* iexx;
+  const R* ieyy;
+  const AxisCoef<R>* ax;
+  const AxisCoef<R>* ay;
+  R S;
+  const R* jx;
+  const R* jy;
+};
+
+template <typename R>
+__global__ void k_te_h(TEArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int ip = i + 1 == a.nx ? 0 : i + 1, jp = j + 1 == a.ny ? 0 : j + 1;
+  const size_t nr = (size_t)i * a.ny + jp, nd = (size_t)ip * a.ny + j;
+  const R ex = a.dx[n] * a.iexx[n], exr = a.dx[nr] * a.iexx[nr];
+  const R ey = a.dy[n] * a.ieyy[n], eyd = a.dy[nd] * a.ieyy[nd];
+  const R ce = (eyd - ey) - (exr - ex);
+  const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
+  const R ph = cx.pH * cy.pH;
+  const R m1 = (R(1) - cx.aH - cy.aH - cx.aH * cy.aH) * ph;
+  const R m2 = -a.S * ph;
+  const R m4 = R(-4) * cx.aH * cy.aH * ph;
+  const R hz = a.hz[n];
+  R ih = R(0);
+  if (m4 != R(0)) { ih = a.ihz[n] + hz; a.ihz[n] = ih; }
+  a.hz[n] = m1 * hz + m2 * ce + m4 * ih;
+}
+
+template <typename R>
+__global__ void k_te_d(TEArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int im = i == 0 ? a.nx - 1 : i - 1, jm = j == 0 ? a.ny - 1 : j - 1;
+  const R hz = a.hz[n];
+  const R chx = hz - a.hz[(size_t)i * a.ny + jm];
+  const R chy = -(hz - a.hz[(size_t)im * a.ny + j]);
+  const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
+  R icx = R(0), icy = R(0);
+  if (cx.aD != R(0)) { icx = a.ichx[n] + chx; a.ichx[n] = icx; }
+  if (cy.aD != R(0)) { icy = a.ichy[n] + chy; a.ichy[n] = icy; }
+  R vx = cy.f1D * a.dx[n] + cy.f2D * (chx + R(2) * cx.aD * icx);
+  R vy = cx.f1D * a.dy[n] + cx.f2D * (chy + R(2) * cy.aD * icy);
+  if (a.jx) vx += a.jx[n];
+  if (a.jy) vy += a.jy[n];
+  a.dx[n] = vx;
+  a.dy[n] = vy;
+}
+
+template <typename R>
+__global__ void k_e_fields(int N, const R* dx, const R* dy, const R* dz, const R* iexx,
+                           const R* ieyy, const R* iez, R* ex, R* ey, R* ez) {
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < (size_t)N;
+       n += (size_t)gridDim.x * blockDim.x) {
+    if (ez) ez[n] = iez[n] * dz[n];
+    if (ex) ex[n] = iexx[n] * dx[n];
+    if (ey) ey[n] = ieyy[n] * dy[n];
+  }
+}
+
+// sparse source injection Dz[idx] += w * amps[t]
+template <typename R>
+__global__ void k_add_src(R* dz, int ns, const int* idx, const R* w, const R* amps, int t) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < ns) dz[idx[k]] += w[k] * amps[t];
+}
+
+template <typename R>
+__global__ void k_probe(const R* dz, const R* iez, int np, const int* idx, R* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < np) out[k] = dz[idx[k]] * iez[idx[k]];
+}
+
+// ------------------------------------------------------- time-blocked TM
+// One CTA advances a TI x TJ tile by K steps in shared memory, computing a
+// halo of K cells that shrinks by one per step (H needs Ez at i+1, j+1; D
+// needs H at i-1, j-1).  State is double-buffered in global memory.
+constexpr int TB_TI = 32, TB_TJ = 32, TB_KMAX = 8, TB_THREADS = 256;
+
+template <typename R>
+struct TBArgs {
+  int nx, ny, K, t0;
+  const R* hx_i; const R* hy_i; const R* dz_i; const R* icex_i; const R* icey_i; const R* idz_i;
+  R* hx_o; R* hy_o; R* dz_o; R* icex_o; R* icey_o; R* idz_o;
+  const R* iez;
+  const AxisCoef<R>* ax;
+  const AxisCoef<R>* ay;
+  R S;
+  int ns;
+  const int* src_idx;
+  const R* src_w;
+  const R* amps;  // amps[t]
+  int np;
+  const int* probe_idx;
+  R* probe_out;   // [t][np]
+};
+
+template <typename R>
+__global__ void __launch_bounds__(TB_THREADS) k_tm_blocked(TBArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const int K = a.K;
+  const int RI = TB_TI + 2 * K, RJ = TB_TJ + 2 * K;
+  const int RN = RI * RJ;
+  R* sHx = (R*)smraw;
+  R* sHy = sHx + RN;
+  R* sDz = sHy + RN;
+  R* sIe = sDz + RN;
+  R* sCx = sIe + RN;  // ICEx'
+  R* sCy = sCx + RN;  // ICEy'
+  R* sId = sCy + RN;  // IDz
+  AxisCoef<R>* cX = (AxisCoef<R>*)(sId + RN);
+  AxisCoef<R>* cY = cX + RI;
+  const int gi0 = blockIdx.y * TB_TI - K;  // region origin (may be negative)
+  const int gj0 = blockIdx.x * TB_TJ - K;
+  const int tid = threadIdx.x;
+  auto gi = [&](int r) { int v = gi0 + r; v %= a.nx; return v < 0 ? v + a.nx : v; };
+  auto gj = [&](int c) { int v = gj0 + c; v %= a.ny; return v < 0 ? v + a.ny : v; };
+  for (int r = tid; r < RI; r += TB_THREADS) cX[r] = a.ax[gi(r)];
+  for (int c = tid; c < RJ; c += TB_THREADS) cY[c] = a.ay[gj(c)];
+  __syncthreads();
+  int pml_local = 0;
+  for (int r = tid; r < RI; r += TB_THREADS) pml_local |= (cX[r].aH != R(0)) | (cX[r].aD != R(0));
+  for (int c = tid; c < RJ; c += TB_THREADS) pml_local |= (cY[c].aH != R(0)) | (cY[c].aD != R(0));
+  const bool pml = __syncthreads_or(pml_local);
+  for (int q = tid; q < RN; q += TB_THREADS) {
+    const int r = q / RJ, c = q - r * RJ;
+    const size_t n = (size_t)gi(r) * a.ny + gj(c);
+    sHx[q] = a.hx_i[n];
+    sHy[q] = a.hy_i[n];
+    sDz[q] = a.dz_i[n];
+    sIe[q] = a.iez[n];
+    if (pml) {
+      sCx[q] = a.icex_i[n];
+      sCy[q] = a.icey_i[n];
+      sId[q] = a.idz_i[n];
+    }
+  }
+  __syncthreads();
+  for (int s = 0; s < K; ++s) {
+    // H phase on [0, RI-1) x [0, RJ-1)
+    for (int q = tid; q < RN; q += TB_THREADS) {
+      const int r = q / RJ, c = q - r * RJ;
+      if (r >= RI - 1 || c >= RJ - 1) continue;
+      const R ez = sDz[q] * sIe[q];
+      const R dEy = sDz[q + 1] * sIe[q + 1] - ez;
+      const R dEx = -(sDz[q + RJ] * sIe[q + RJ] - ez);
+      const AxisCoef<R> cx = cX[r], cy = cY[c];
+      R icx = R(0), icy = R(0);
+      if (pml) {
+        if (cx.aH != R(0)) { icx = sCx[q] + dEy; sCx[q] = icx; }
+        if (cy.aH != R(0)) { icy = sCy[q] + dEx; sCy[q] = icy; }
+      }
+      sHx[q] = cy.f1H * sHx[q] - cy.f2H * (dEy + R(2) * cx.aH * icx);
+      sHy[q] = cx.f1H * sHy[q] - cx.f2H * (dEx + R(2) * cy.aH * icy);
+    }
+    __syncthreads();
+    // D phase on [1, RI) x [1, RJ)
+    for (int q = tid; q < RN; q += TB_THREADS) {
+      const int r = q / RJ, c = q - r * RJ;
+      if (r < 1 || c < 1) continue;
+      const R ch = (sHy[q] - sHy[q - RJ]) - (sHx[q] - sHx[q - 1]);
+      R m1, m2, m4;
+      dz_coefs(cX[r], cY[c], a.S, m1, m2, m4);
+      const R dz = sDz[q];
+      R id = R(0);
+      if (pml && m4 != R(0)) { id = sId[q] + dz; sId[q] = id; }
+      sDz[q] = m1 * dz + m2 * ch + m4 * id;
+    }
+    __syncthreads();
+    const int t = a.t0 + s;
+    if (a.ns > 0) {
+      const R amp = a.amps[t];
+      for (int k = tid; k < a.ns; k += TB_THREADS) {
+        const int n = a.src_idx[k];
+        const int ii = n / a.ny, jj = n - ii * a.ny;
+        int r = (ii - gi0) % a.nx; if (r < 0) r += a.nx;
+        int c = (jj - gj0) % a.ny; if (c < 0) c += a.ny;
+        if (r < RI && c < RJ) sDz[r * RJ + c] += a.src_w[k] * amp;
+      }
+      __syncthreads();
+    }
+    for (int k = tid; k < a.np; k += TB_THREADS) {
+      const int n = a.probe_idx[k];
+      const int ii = n / a.ny, jj = n - ii * a.ny;
+      const int r = ii - gi0, c = jj - gj0;
+      if (r >= K && r < K + TB_TI && c >= K && c < K + TB_TJ) {
+        const int q = r * RJ + c;
+        a.probe_out[(size_t)t * a.np + k] = sDz[q] * sIe[q];
+      }
+    }
+  }
+  // write back the tile interior
+  for (int q = tid; q < TB_TI * TB_TJ; q += TB_THREADS) {
+    const int r = q / TB_TJ + K, c = q % TB_TJ + K;
+    const int ii = gi0 + r, jj = gj0 + c;
+    if (ii >= a.nx || jj >= a.ny) continue;
+    const size_t n = (size_t)ii * a.ny + jj;
+    const int p = r * RJ + c;
+    a.hx_o[n] = sHx[p];
+    a.hy_o[n] = sHy[p];
+    a.dz_o[n] = sDz[p];
+    if (pml) {
+      a.icex_o[n] = sCx[p];
+      a.icey_o[n] = sCy[p];
+      a.idz_o[n] = sId[p];
+    }
+  }
+}
+
+template <typename R>
+static size_t tb_smem(int K) {
+  const int RI = TB_TI + 2 * K, RJ = TB_TJ + 2 * K;
+  return (size_t)7 * RI * RJ * sizeof(R) + (size_t)(RI + RJ) * sizeof(AxisCoef<R>);
+}
+
+// ------------------------------------------------------------ TM adjoint
+// Reverse of one TM step n (see header comment for the forward form):
+//   aCH = m2 aDz ; aIDz += m4 aDz ; aDz_prev = m1 aDz + aIDz
+//   aHy_t = aHy + aCH - aCH[i+1,j] ; aHx_t = aHx - (aCH - aCH[i,j+1])
+//   aHx = f1Hy aHx_t ; t = -f2Hy aHx_t ; aICEx += 2aHx t ; adEy = t + aICEx  (same for y)
+//   aEz^{n-1} = w_{n-1} p + adEy[i,j-1] - adEy + adEx - adEx[i-1,j]
+//   aDz^{n-1} = aDz_prev + aEz^{n-1}/eps ; geps += aEz^{n-1} (-Dz^{n-1}/eps^2)
+template <typename R>
+struct AdjArgs {
+  int nx, ny;
+  R* ahx; R* ahy; R* adz; R* aicex; R* aicey; R* aidz;
+  R* ach; R* adey; R* adex; R* adzp;
+  const R* iez;
+  const AxisCoef<R>* ax;
+  const AxisCoef<R>* ay;
+  R S;
+};
+
+template <typename R>
+__global__ void k_adj_a(AdjArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  R m1, m2, m4;
+  dz_coefs(a.ax[i], a.ay[j], a.S, m1, m2, m4);
+  const R adz = a.adz[n];
+  a.ach[n] = m2 * adz;
+  R aid = a.aidz[n];
+  if (m4 != R(0)) { aid += m4 * adz; a.aidz[n] = aid; }
+  a.adzp[n] = m1 * adz + aid;
+}
+
+template <typename R>
+__global__ void k_adj_b(AdjArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int ip = i + 1 == a.nx ? 0 : i + 1, jp = j + 1 == a.ny ? 0 : j + 1;
+  const R ach = a.ach[n];
+  const R ahy_t = a.ahy[n] + ach - a.ach[(size_t)ip * a.ny + j];
+  const R ahx_t = a.ahx[n] - (ach - a.ach[(size_t)i * a.ny + jp]);
+  const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
+  a.ahx[n] = cy.f1H * ahx_t;
+  R t = -cy.f2H * ahx_t;
+  R ai = R(0);
+  if (cx.aH != R(0)) { ai = a.aicex[n] + R(2) * cx.aH * t; a.aicex[n] = ai; }
+  a.adey[n] = t + ai;
+  a.ahy[n] = cx.f1H * ahy_t;
+  t = -cx.f2H * ahy_t;
+  ai = R(0);
+  if (cy.aH != R(0)) { ai = a.aicey[n] + R(2) * cy.aH * t; a.aicey[n] = ai; }
+  a.adex[n] = t + ai;
+}
+
+// finishes the step: aDz for Ez^{n-1}; gradient term with Dz^{n-1}
+template <typename R>
+__global__ void k_adj_c(AdjArgs<R> a, const R* dz_prev, double* geps, int np, const int* pidx,
+                        const R* wrow) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int im = i == 0 ? a.nx - 1 : i - 1, jm = j == 0 ? a.ny - 1 : j - 1;
+  R aez = a.adey[(size_t)i * a.ny + jm] - a.adey[n] + a.adex[n] - a.adex[(size_t)im * a.ny + j];
+  if (wrow) {
+    for (int k = 0; k < np; ++k)
+      if (pidx[k] == (int)n) aez += wrow[k];
+  }
+  const R ie = a.iez[n];
+  a.adz[n] = a.adzp[n] + aez * ie;
+  if (dz_prev) geps[n] += (double)aez * (double)(-dz_prev[n] * ie * ie);
+}
+
+// initial adjoint for the last output step T: aEz^T = w_T p
+template <typename R>
+__global__ void k_adj_init(int N, R* adz, const R* iez, double* geps, const R* dz_T, int np,
+                           const int* pidx, const R* wrow) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  const int n = pidx[k];
+  const R ie = iez[n];
+  atomicAdd(&adz[n], wrow[k] * ie);
+  atomicAdd(&geps[n], (double)wrow[k] * (double)(-dz_T[n] * ie * ie));
+}
+
+dim3 grid2(int nx, int ny, dim3 blk) { return dim3((ny + blk.x - 1) / blk.x, (nx + blk.y - 1) / blk.y, 1); }
+
+template <typename R>
+TMArgs<R> tm_args(cev_fdtd_plan p, const cev_fdtd_state* st, const R* jz) {
+  TMArgs<R> a;
+  a.nx = p->nx;
+  a.ny = p->ny;
+  a.hx = (R*)st->hx; a.hy = (R*)st->hy; a.dz = (R*)st->dz;
+  a.icex = (R*)st->icex; a.icey = (R*)st->icey; a.idz = (R*)st->idz;
+  a.iez = (const R*)p->iez;
+  a.ax = (const AxisCoef<R>*)p->ax;
+  a.ay = (const AxisCoef<R>*)p->ay;
+  a.S = (R)p->S;
+  a.jz = jz;
+  return a;
+}
+
+template <typename R>
+int step_impl(cev_fdtd_plan p, const cev_fdtd_state* st, const R* jx, const R* jy, const R* jz,
+              int te, cudaStream_t s) {
+  const dim3 blk(32, 8);
+  const dim3 g = grid2(p->nx, p->ny, blk);
+  TMArgs<R> a = tm_args<R>(p, st, jz);
+  k_tm_h<R><<<g, blk, 0, s>>>(a);
+  if (te) {
+    TEArgs<R> e;
+    e.nx = p->nx; e.ny = p->ny;
+    e.hz = (R*)st->hz; e.dx = (R*)st->dx; e.dy = (R*)st->dy;
+    e.ihz = (R*)st->ihz; e.ichx = (R*)st->ichx; e.ichy = (R*)st->ichy;
+    e.iexx = (const R*)p->iexx; e.ieyy = (const R*)p->ieyy;
+    e.ax = a.ax; e.ay = a.ay; e.S = a.S; e.jx = jx; e.jy = jy;
+    k_te_h<R><<<g, blk, 0, s>>>(e);
+    k_te_d<R><<<g, blk, 0, s>>>(e);
+  }
+  k_tm_d<R><<<g, blk, 0, s>>>(a);
+  CEV_CHECK_LAUNCH("fdtd step");
+  return CEV_OK;
+}
+
+template <typename R>
+int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev_fdtd_io* io,
+                cudaStream_t s) {
+  const size_t N = p->n();
+  const int ns = io ? io->n_src : 0, np = io ? io->n_probe : 0;
+  const bool blocked = p->nx >= TB_TI + 2 * TB_KMAX && p->ny >= TB_TJ + 2 * TB_KMAX;
+  if (!blocked) {
+    // small grids: per-step kernels
+    for (int t = 0; t < nsteps; ++t) {
+      int rc = step_impl<R>(p, st, nullptr, nullptr, nullptr, 0, s);
+      if (rc != CEV_OK) return rc;
+      if (ns > 0)
+        k_add_src<R><<<(ns + 127) / 128, 128, 0, s>>>((R*)st->dz, ns, io->src_idx,
+                                                       (const R*)io->src_w, (const R*)io->amps, t);
+      if (np > 0)
+        k_probe<R><<<(np + 127) / 128, 128, 0, s>>>((const R*)st->dz, (const R*)p->iez, np,
+                                                     io->probe_idx, (R*)io->probe_out + (size_t)t * np);
+    }
+    CEV_CHECK_LAUNCH("fdtd run (per step)");
+    return CEV_OK;
+  }
+  if (!p->shadow) CEV_CUDA(cudaMalloc(&p->shadow, 6 * N * sizeof(R)));
+  R* sh = (R*)p->shadow;
+  R* bufA[6] = {(R*)st->hx, (R*)st->hy, (R*)st->dz, (R*)st->icex, (R*)st->icey, (R*)st->idz};
+  R* bufB[6] = {sh, sh + N, sh + 2 * N, sh + 3 * N, sh + 4 * N, sh + 5 * N};
+  // the shadow's PML integrals must match the state outside tiles that skip them
+  CEV_CUDA(cudaMemcpyAsync(bufB[3], bufA[3], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+  CEV_CUDA(cudaMemcpyAsync(bufB[4], bufA[4], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+  CEV_CUDA(cudaMemcpyAsync(bufB[5], bufA[5], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+  const int K = TB_KMAX;
+  const size_t smem = tb_smem<R>(K);
+  static bool attr_set[2] = {false, false};
+  if (!attr_set[sizeof(R) == 8]) {
+    CEV_CUDA(cudaFuncSetAttribute(k_tm_blocked<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tb_smem<R>(TB_KMAX)));
+    attr_set[sizeof(R) == 8] = true;
+  }
+  const dim3 g((p->ny + TB_TJ - 1) / TB_TJ, (p->nx + TB_TI - 1) / TB_TI, 1);
+  R** in = bufA;
+  R** out = bufB;
+  int t = 0;
+  while (t < nsteps) {
+    const int k = std::min(K, nsteps - t);
+    TBArgs<R> a;
+    a.nx = p->nx; a.ny = p->ny; a.K = k; a.t0 = t;
+    a.hx_i = in[0]; a.hy_i = in[1]; a.dz_i = in[2]; a.icex_i = in[3]; a.icey_i = in[4]; a.idz_i = in[5];
+    a.hx_o = out[0]; a.hy_o = out[1]; a.dz_o = out[2]; a.icex_o = out[3]; a.icey_o = out[4]; a.idz_o = out[5];
+    a.iez = (const R*)p->iez;
+    a.ax = (const AxisCoef<R>*)p->ax;
+    a.ay = (const AxisCoef<R>*)p->ay;
+    a.S = (R)p->S;
+    a.ns = ns;
+    a.src_idx = ns ? io->src_idx : nullptr;
+    a.src_w = ns ? (const R*)io->src_w : nullptr;
+    a.amps = ns ? (const R*)io->amps : nullptr;
+    a.np = np;
+    a.probe_idx = np ? io->probe_idx : nullptr;
+    a.probe_out = np ? (R*)io->probe_out : nullptr;
+    k_tm_blocked<R><<<g, TB_THREADS, smem, s>>>(a);
+    CEV_CHECK_LAUNCH("k_tm_blocked");
+    std::swap(in, out);
+    t += k;
+  }
+  if (in != bufA)
+    for (int f = 0; f < 6; ++f)
+      CEV_CUDA(cudaMemcpyAsync(bufA[f], in[f], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+  return CEV_OK;
+}
+
+template <typename R>
+int adjoint_impl(cev_fdtd_plan p, int T, int C, const cev_fdtd_io* io, const R* w, double* geps,
+                 void* ws, cudaStream_t s) {
+  const size_t N = p->n();
+  const int nck = (T + C - 1) / C + 1;
+  R* base = (R*)ws;
+  R* cur[6];
+  for (int f = 0; f < 6; ++f) cur[f] = base + f * N;
+  R* ck = base + 6 * N;                    // nck checkpoints of 6 fields
+  R* seg = ck + (size_t)nck * 6 * N;       // (C+1) Dz snapshots
+  R* adj = seg + (size_t)(C + 1) * N;      // 10 adjoint arrays
+  const int ns = io->n_src, np = io->n_probe;
+  cev_fdtd_state st{};
+  st.hx = cur[0]; st.hy = cur[1]; st.dz = cur[2]; st.icex = cur[3]; st.icey = cur[4]; st.idz = cur[5];
+  CEV_CUDA(cudaMemsetAsync(base, 0, 6 * N * sizeof(R), s));
+  CEV_CUDA(cudaMemsetAsync(adj, 0, 10 * N * sizeof(R), s));
+  auto fwd_step = [&](int t) -> int {
+    int rc = step_impl<R>(p, &st, nullptr, nullptr, nullptr, 0, s);
+    if (rc != CEV_OK) return rc;
+    if (ns > 0)
+      k_add_src<R><<<(ns + 127) / 128, 128, 0, s>>>(cur[2], ns, io->src_idx, (const R*)io->src_w,
+                                                     (const R*)io->amps, t);
+    return CEV_OK;
+  };
+  // forward sweep with checkpoints of the state before steps 0, C, 2C, ...
+  for (int t = 0; t < T; ++t) {
+    if (t % C == 0)
+      CEV_CUDA(cudaMemcpyAsync(ck + (size_t)(t / C) * 6 * N, base, 6 * N * sizeof(R),
+                               cudaMemcpyDeviceToDevice, s));
+    int rc = fwd_step(t);
+    if (rc != CEV_OK) return rc;
+  }
+  AdjArgs<R> a;
+  a.nx = p->nx; a.ny = p->ny;
+  a.ahx = adj; a.ahy = adj + N; a.adz = adj + 2 * N; a.aicex = adj + 3 * N; a.aicey = adj + 4 * N;
+  a.aidz = adj + 5 * N; a.ach = adj + 6 * N; a.adey = adj + 7 * N; a.adex = adj + 8 * N;
+  a.adzp = adj + 9 * N;
+  a.iez = (const R*)p->iez;
+  a.ax = (const AxisCoef<R>*)p->ax;
+  a.ay = (const AxisCoef<R>*)p->ay;
+  a.S = (R)p->S;
+  const dim3 blk(32, 8);
+  const dim3 g = grid2(p->nx, p->ny, blk);
+  bool first = true;
+  for (int seg0 = ((T - 1) / C) * C; seg0 >= 0; seg0 -= C) {
+    const int seg1 = std::min(T, seg0 + C);
+    // recompute Dz^{seg0} .. Dz^{seg1} (Dz^t = Dz after step t; index t - seg0)
+    CEV_CUDA(cudaMemcpyAsync(base, ck + (size_t)(seg0 / C) * 6 * N, 6 * N * sizeof(R),
+                             cudaMemcpyDeviceToDevice, s));
+    CEV_CUDA(cudaMemcpyAsync(seg, cur[2], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+    for (int t = seg0; t < seg1; ++t) {
+      int rc = fwd_step(t);
+      if (rc != CEV_OK) return rc;
+      CEV_CUDA(cudaMemcpyAsync(seg + (size_t)(t + 1 - seg0) * N, cur[2], N * sizeof(R),
+                               cudaMemcpyDeviceToDevice, s));
+    }
+    if (first) {
+      // output step T (after the last step): aEz^T = w[T-1] p
+      k_adj_init<R><<<(np + 127) / 128, 128, 0, s>>>((int)N, a.adz, a.iez, geps,
+                                                       seg + (size_t)(T - seg0) * N, np,
+                                                       io->probe_idx, w + (size_t)(T - 1) * np);
+      first = false;
+    }
+    // reverse steps n = seg1 .. seg0+1 (step n maps state n-1 -> n)
+    for (int n = seg1; n > seg0; --n) {
+      k_adj_a<R><<<g, blk, 0, s>>>(a);
+      k_adj_b<R><<<g, blk, 0, s>>>(a);
+      // Ez^{n-1}: output of step n-1 (weights w[n-2]); n-1 == 0 is the initial field
+      const R* wrow = (n - 1 >= 1) ? w + (size_t)(n - 2) * np : nullptr;
+      const R* dzp = (n - 1 >= 1) ? seg + (size_t)(n - 1 - seg0) * N : nullptr;
+      k_adj_c<R><<<g, blk, 0, s>>>(a, dzp, geps, np, io->probe_idx, wrow);
+    }
+    CEV_CHECK_LAUNCH("fdtd adjoint segment");
+  }
+  return CEV_OK;
+}
+
+}  // namespace cev
+
+using namespace cev;
+
+extern "C" {
+
+int cev_fdtd_plan_create(cev_fdtd_plan* out, int nx, int ny, double dL, int npml_x, int npml_y,
+                         int precision, const double* eps, cudaStream_t s) {
+  CEV_REQUIRE(out != nullptr, "plan output pointer is NULL");
+  *out = nullptr;
+  CEV_REQUIRE(nx >= 2 && ny >= 2, "grid (%d, %d) must be at least 2x2", nx, ny);
+  CEV_REQUIRE((long)nx * ny <= (1L << 31) - 1, "grid too large");
+  CEV_REQUIRE(dL > 0 && std::isfinite(dL), "dL must be positive");
+  CEV_REQUIRE(npml_x >= 0 && npml_y >= 0 && 2 * npml_x <= nx && 2 * npml_y <= ny,
+              "npml (%d, %d) must be >= 0 and fit twice in the grid", npml_x, npml_y);
+  CEV_REQUIRE(precision == CEV_PREC_C64 || precision == CEV_PREC_C128, "bad precision");
+  CEV_REQUIRE(eps != nullptr, "eps is NULL");
+  auto* p = new cev_fdtd_plan_s();
+  p->nx = nx; p->ny = ny; p->npml_x = npml_x; p->npml_y = npml_y; p->prec = precision;
+  p->dL = dL;
+  p->dt = fdtd_dt(dL);
+  const double C_0 = 1.0 / std::sqrt(F_EPSILON_0 * F_MU_0);
+  p->S = C_0 * p->dt / dL;
+  sigma_profile(nx, npml_x, p->dt, p->aHx, p->aDx);
+  sigma_profile(ny, npml_y, p->dt, p->aHy, p->aDy);
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void** dst, const void* src, size_t bytes) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc(dst, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  if (precision == CEV_PREC_C128) {
+    auto cx = axis_coefs<double>(p->aHx, p->aDx, p->S), cy = axis_coefs<double>(p->aHy, p->aDy, p->S);
+    up(&p->ax, cx.data(), cx.size() * sizeof(cx[0]));
+    up(&p->ay, cy.data(), cy.size() * sizeof(cy[0]));
+  } else {
+    auto cx = axis_coefs<float>(p->aHx, p->aDx, p->S), cy = axis_coefs<float>(p->aHy, p->aDy, p->S);
+    up(&p->ax, cx.data(), cx.size() * sizeof(cx[0]));
+    up(&p->ay, cy.data(), cy.size() * sizeof(cy[0]));
+  }
+  const size_t N = p->n();
+  if (e == cudaSuccess) e = cudaMalloc(&p->iez, N * p->rs());
+  if (e == cudaSuccess) e = cudaMalloc(&p->iexx, N * p->rs());
+  if (e == cudaSuccess) e = cudaMalloc(&p->ieyy, N * p->rs());
+  if (e != cudaSuccess) {
+    cev_fdtd_plan_destroy(p);
+    return cuda_status(e, "cev_fdtd_plan_create");
+  }
+  int rc = cev_fdtd_set_eps(p, eps, s);
+  if (rc != CEV_OK) {
+    cev_fdtd_plan_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return CEV_OK;
+}
+
+int cev_fdtd_plan_destroy(cev_fdtd_plan p) {
+  if (!p) return CEV_OK;
+  cudaFree(p->ax);
+  cudaFree(p->ay);
+  cudaFree(p->iez);
+  cudaFree(p->iexx);
+  cudaFree(p->ieyy);
+  cudaFree(p->shadow);
+  delete p;
+  return CEV_OK;
+}
+
+int cev_fdtd_set_eps(cev_fdtd_plan p, const double* eps, cudaStream_t s) {
+  CEV_REQUIRE(p && eps, "NULL argument");
+  const size_t N = p->n();
+  const unsigned g = std::max(1u, std::min(ceil_div(N, 256), 8u * sm_count()));
+  if (p->prec == CEV_PREC_C128)
+    k_inv_eps<double><<<g, 256, 0, s>>>(eps, (double*)p->iez, (double*)p->iexx, (double*)p->ieyy,
+                                        p->nx, p->ny);
+  else
+    k_inv_eps<float><<<g, 256, 0, s>>>(eps, (float*)p->iez, (float*)p->iexx, (float*)p->ieyy,
+                                       p->nx, p->ny);
+  CEV_CHECK_LAUNCH("k_inv_eps");
+  return CEV_OK;
+}
+
+double cev_fdtd_dt(cev_fdtd_plan p) { return p ? p->dt : 0.0; }
+
+int cev_fdtd_step(cev_fdtd_plan p, const cev_fdtd_state* st, const void* jx, const void* jy,
+                  const void* jz, int te, cudaStream_t s) {
+  CEV_REQUIRE(p && st, "NULL argument");
+  CEV_REQUIRE(st->hx && st->hy && st->dz && st->icex && st->icey && st->idz, "TM state incomplete");
+  if (te || jx || jy) {
+    CEV_REQUIRE(st->hz && st->dx && st->dy && st->ihz && st->ichx && st->ichy,
+                "TE state incomplete");
+    te = 1;
+  }
+  if (p->prec == CEV_PREC_C128)
+    return step_impl<double>(p, st, (const double*)jx, (const double*)jy, (const double*)jz, te, s);
+  return step_impl<float>(p, st, (const float*)jx, (const float*)jy, (const float*)jz, te, s);
+}
+
+int cev_fdtd_e_fields(cev_fdtd_plan p, const cev_fdtd_state* st, void* ex, void* ey, void* ez,
+                      cudaStream_t s) {
+  CEV_REQUIRE(p && st, "NULL argument");
+  CEV_REQUIRE(!ez || st->dz, "ez needs st->dz");
+  CEV_REQUIRE(!(ex || ey) || (st->dx && st->dy), "ex/ey need st->dx, st->dy");
+  const size_t N = p->n();
+  const unsigned g = std::max(1u, std::min(ceil_div(N, 256), 8u * sm_count()));
+  if (p->prec == CEV_PREC_C128)
+    k_e_fields<double><<<g, 256, 0, s>>>((int)N, (const double*)st->dx, (const double*)st->dy,
+                                         (const double*)st->dz, (const double*)p->iexx,
+                                         (const double*)p->ieyy, (const double*)p->iez,
+                                         (double*)ex, (double*)ey, (double*)ez);
+  else
+    k_e_fields<float><<<g, 256, 0, s>>>((int)N, (const float*)st->dx, (const float*)st->dy,
+                                        (const float*)st->dz, (const float*)p->iexx,
+                                        (const float*)p->ieyy, (const float*)p->iez, (float*)ex,
+                                        (float*)ey, (float*)ez);
+  CEV_CHECK_LAUNCH("k_e_fields");
+  return CEV_OK;
+}
+
+int cev_fdtd_run_tm(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev_fdtd_io* io,
+                    cudaStream_t s) {
+  CEV_REQUIRE(p && st, "NULL argument");
+  CEV_REQUIRE(nsteps >= 0, "nsteps must be >= 0");
+  CEV_REQUIRE(st->hx && st->hy && st->dz && st->icex && st->icey && st->idz, "TM state incomplete");
+  if (io) {
+    CEV_REQUIRE(io->n_src >= 0 && io->n_probe >= 0, "negative source/probe count");
+    CEV_REQUIRE(io->n_src == 0 || (io->src_idx && io->src_w && io->amps), "source arrays missing");
+    CEV_REQUIRE(io->n_probe == 0 || (io->probe_idx && io->probe_out), "probe arrays missing");
+  }
+  if (nsteps == 0) return CEV_OK;
+  if (p->prec == CEV_PREC_C128) return run_tm_impl<double>(p, st, nsteps, io, s);
+  return run_tm_impl<float>(p, st, nsteps, io, s);
+}
+
+size_t cev_fdtd_adjoint_workspace_size(cev_fdtd_plan p, int nsteps, int C) {
+  if (!p || nsteps < 1 || C < 1) return 0;
+  const size_t N = p->n();
+  const size_t nck = (nsteps + C - 1) / C + 1;
+  return (6 + nck * 6 + (size_t)(C + 1) + 10) * N * p->rs();
+}
+
+int cev_fdtd_adjoint_tm(cev_fdtd_plan p, int nsteps, int C, const cev_fdtd_io* io, const void* w,
+                        double* geps, void* ws, size_t ws_bytes, cudaStream_t s) {
+  CEV_REQUIRE(p && io && w && geps && ws, "NULL argument");
+  CEV_REQUIRE(nsteps >= 1 && C >= 1, "nsteps and ckpt_every must be >= 1");
+  CEV_REQUIRE(io->n_probe >= 1 && io->probe_idx, "adjoint needs probes");
+  CEV_REQUIRE(io->n_src == 0 || (io->src_idx && io->src_w && io->amps), "source arrays missing");
+  const size_t need = cev_fdtd_adjoint_workspace_size(p, nsteps, C);
+  CEV_REQUIRE(ws_bytes >= need, "workspace too small: need %zu bytes, got %zu", need, ws_bytes);
+  if (p->prec == CEV_PREC_C128)
+    return adjoint_impl<double>(p, nsteps, C, io, (const double*)w, geps, ws, s);
+  return adjoint_impl<float>(p, nsteps, C, io, (const float*)w, geps, ws, s);
+}
+
+}  // extern "C"

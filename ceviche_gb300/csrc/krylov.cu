@@ -1,0 +1,657 @@
+// Restarted (flexible) GMRES on the matrix-free SC-PML stencil.
+//
+// Precision split: Arnoldi vectors, the stencil inside the cycle and the
+// orthogonalisation run in complex64; inner products are reduced across
+// threads and blocks in FP64 in a fixed order (deterministic); the
+// Hessenberg matrix, Givens rotations and the small triangular solve are
+// FP64 on the device; every restart recomputes the true residual
+// b - A x in FP64 from the complex128 iterate and adds the cycle's
+// correction to x in FP64 (mixed-precision iterative refinement).
+//
+// Device-side control: each problem of the batch carries a KState; the last
+// block of a reduction (threadfence + counter) finalises the per-problem
+// scalars, so a whole cycle is enqueued without host round trips.  The host
+// reads the FP64 residuals once per cycle.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fdfd_plan.hpp"
+#include "krylov.hpp"
+
+namespace cev {
+
+void launch_geometry(int nx, int ny, int batch, dim3& grid, dim3& block, int& rows);
+
+static constexpr int RED_THREADS = 256;
+static constexpr int DOT_GROUP = 16;
+
+// --------------------------------------------------------------- reductions
+// Block-wide sum of NV doubles per thread into out (valid in thread 0).
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* smem /* NV*32 */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = v[k];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = lane < nw ? smem[k * 32 + lane] : 0.0;
+      v[k] = warp_sum(t);
+    }
+  }
+}
+
+// Arrival counter: returns true in the whole block of the last block to
+// arrive (after its partials are visible).  Resets the counter.
+__device__ __forceinline__ bool last_block(unsigned* counter, unsigned nblocks) {
+  __shared__ bool s_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    const unsigned t = atomicAdd(counter, 1u);
+    s_last = (t == nblocks - 1);
+    if (s_last) *counter = 0u;
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
+}
+
+// --------------------------------------------------------------- residual
+template <int POL>
+struct ResArgs {
+  int nx, ny, rows, first, m;
+  const double* eps;
+  size_t eps_bs;
+  const double2* x;
+  const double2* b;
+  double bscale;
+  const Coef<double>* cx;
+  const Coef<double>* cy;
+  const double* k2;
+  float2* r;  // V_0 slot of each problem (stride n)
+  size_t r_bs;
+  KCtx ctx;
+};
+
+template <int POL>
+__global__ void __launch_bounds__(128) k_residual(ResArgs<POL> a) {
+  const int b = blockIdx.z;
+  KState* st = a.ctx.st + b;
+  if (st->done) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t N = (size_t)a.nx * a.ny;
+  const unsigned nblk = gridDim.x * gridDim.y;
+  const unsigned blk = blockIdx.y * gridDim.x + blockIdx.x;
+  double acc[2] = {0.0, 0.0};
+  if (j < a.ny) {
+    const int i0 = blockIdx.y * a.rows;
+    const int i1 = min(i0 + a.rows, a.nx);
+    const double2* x = a.x + b * N;
+    const double2* bb = a.b + b * N;
+    float2* r = a.r + b * a.r_bs;
+    const Coef<double> cyj = a.cy[(size_t)b * a.ny + j];
+    const double bs = a.bscale;
+    auto ep = [&](int i, double2 v, double2) {
+      const size_t n = (size_t)i * a.ny + j;
+      const double2 bv = cscale(bb[n], bs);
+      const double2 rv = csub(bv, v);
+      r[n] = to_f(rv);
+      acc[0] += rv.x * rv.x + rv.y * rv.y;
+      acc[1] += bv.x * bv.x + bv.y * bv.y;
+    };
+    stencil_column<double, POL>(a.nx, a.ny, j, i0, i1, x, a.eps + b * a.eps_bs,
+                                a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
+  }
+  __shared__ double sm[2 * 32];
+  block_sum<2>(acc, sm);
+  double* part = a.ctx.partial + (size_t)b * a.ctx.part_stride;
+  if (threadIdx.x == 0) {
+    part[2 * blk] = acc[0];
+    part[2 * blk + 1] = acc[1];
+  }
+  if (!last_block(a.ctx.counter + 2 * b, nblk)) return;
+  double s[2] = {0.0, 0.0};
+  for (unsigned k = threadIdx.x; k < nblk; k += blockDim.x) {
+    s[0] += __ldcg(part + 2 * k);
+    s[1] += __ldcg(part + 2 * k + 1);
+  }
+  block_sum<2>(s, sm);
+  if (threadIdx.x == 0) {
+    const double beta = sqrt(s[0]);
+    if (a.first) st->bnorm = sqrt(s[1]);
+    st->beta = beta;
+    st->res_est = beta;
+    st->ncols = 0;
+    const int m = a.m;
+    a.ctx.sc[(size_t)b * (m + 1)] = beta > 0 ? 1.0 / beta : 0.0;
+    a.ctx.gam[(size_t)b * (m + 1)] = make_double2(beta, 0.0);
+    st->thresh = fmax(a.ctx.tol * st->bnorm * 0.5, a.ctx.inner_rtol * beta);
+    const bool ok = isfinite(beta);
+    if (!ok) st->nan = 1;
+    st->active = (ok && beta > a.ctx.tol * st->bnorm && st->bnorm > 0) ? 1 : 0;
+  }
+}
+
+// ------------------------------------------------------- Arnoldi matvec
+template <int POL>
+struct MvArgs {
+  int nx, ny, rows, m, j;
+  const float* eps;
+  size_t eps_bs;
+  const float2* in;  // [B][N] with stride in_bs
+  size_t in_bs;
+  int use_scale;     // multiply by sc[b][j]
+  float2* out;
+  size_t out_bs;
+  const Coef<float>* cx;
+  const Coef<float>* cy;
+  const float* k2;
+  KCtx ctx;
+};
+
+template <int POL>
+__global__ void __launch_bounds__(128) k_arnoldi_mv(MvArgs<POL> a) {
+  const int b = blockIdx.z;
+  if (!a.ctx.st[b].active) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.ny) return;
+  const int i0 = blockIdx.y * a.rows;
+  const int i1 = min(i0 + a.rows, a.nx);
+  const float2* x = a.in + b * a.in_bs;
+  float2* y = a.out + b * a.out_bs;
+  const float s = a.use_scale ? (float)a.ctx.sc[(size_t)b * (a.m + 1) + a.j] : 1.0f;
+  const Coef<float> cyj = a.cy[(size_t)b * a.ny + j];
+  auto ep = [&](int i, float2 v, float2) { y[(size_t)i * a.ny + j] = cscale(v, s); };
+  stencil_column<float, POL>(a.nx, a.ny, j, i0, i1, x, a.eps + b * a.eps_bs,
+                             a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
+}
+
+// ----------------------------------------------------------- multi-dot
+// d_k = sum_n conj(V_k[n]) w[n], k = 0..j ; H[j][k] (+)= sc_k d_k
+struct DotArgs {
+  size_t n;
+  int B, m, j, accumulate;
+  const float2* V;  // V_k of problem b at V + (k*B + b)*n
+  KCtx ctx;
+};
+
+__global__ void __launch_bounds__(RED_THREADS) k_multidot(DotArgs a) {
+  const int b = blockIdx.y;
+  KState* st = a.ctx.st + b;
+  if (!st->active) return;
+  const int nv = a.j + 1;
+  const unsigned nblk = gridDim.x;
+  const float2* w = a.V + ((size_t)(a.j + 1) * a.B + b) * a.n;
+  __shared__ double sm[2 * DOT_GROUP * 32];
+  double* part = a.ctx.partial + (size_t)b * a.ctx.part_stride;
+  const size_t stride = (size_t)nblk * blockDim.x;
+  for (int g0 = 0; g0 < nv; g0 += DOT_GROUP) {
+    float2 acc[DOT_GROUP];
+#pragma unroll
+    for (int k = 0; k < DOT_GROUP; ++k) acc[k] = make_float2(0.f, 0.f);
+    for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
+      const float2 wv = w[n];
+#pragma unroll
+      for (int k = 0; k < DOT_GROUP; ++k) {
+        if (g0 + k < nv) {
+          const float2 v = a.V[((size_t)(g0 + k) * a.B + b) * a.n + n];
+          acc[k].x += v.x * wv.x + v.y * wv.y;
+          acc[k].y += v.x * wv.y - v.y * wv.x;
+        }
+      }
+    }
+    double dv[2 * DOT_GROUP];
+#pragma unroll
+    for (int k = 0; k < DOT_GROUP; ++k) {
+      dv[2 * k] = acc[k].x;
+      dv[2 * k + 1] = acc[k].y;
+    }
+    block_sum<2 * DOT_GROUP>(dv, sm);
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < DOT_GROUP && g0 + k < nv; ++k) {
+        part[(size_t)blockIdx.x * 2 * (a.m + 1) + 2 * (g0 + k)] = dv[2 * k];
+        part[(size_t)blockIdx.x * 2 * (a.m + 1) + 2 * (g0 + k) + 1] = dv[2 * k + 1];
+      }
+    }
+    __syncthreads();
+  }
+  if (!last_block(a.ctx.counter + 2 * b, nblk)) return;
+  // fixed-order reduction over blocks, one vector k per thread
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (unsigned q = 0; q < nblk; ++q) {
+      re += __ldcg(part + (size_t)q * 2 * (a.m + 1) + 2 * k);
+      im += __ldcg(part + (size_t)q * 2 * (a.m + 1) + 2 * k + 1);
+    }
+    const double s = a.ctx.sc[(size_t)b * (a.m + 1) + k];
+    const double2 h = make_double2(s * re, s * im);
+    double2* Hc = a.ctx.H + ((size_t)b * a.m + a.j) * (a.m + 1);  // column j
+    a.ctx.hpass[(size_t)b * (a.m + 1) + k] = h;
+    Hc[k] = a.accumulate ? cadd(Hc[k], h) : h;
+  }
+}
+
+// ------------------------------------------------------------ update
+// w -= sum_k V_k (sc_k h_k); final pass: ||w|| -> Givens -> residual estimate
+struct UpdArgs {
+  size_t n;
+  int B, m, j, final_pass;
+  float2* V;
+  KCtx ctx;
+};
+
+__device__ void givens_finish(const UpdArgs& a, int b, double hn) {
+  KCtx& c = const_cast<KCtx&>(a.ctx);
+  KState* st = c.st + b;
+  const int m = a.m, j = a.j;
+  double2* Hc = c.H + ((size_t)b * m + j) * (m + 1);
+  double* cs = c.cs + (size_t)b * m;
+  double2* sn = c.sn + (size_t)b * m;
+  double2* gam = c.gam + (size_t)b * (m + 1);
+  Hc[j + 1] = make_double2(hn, 0.0);
+  for (int k = 0; k < j; ++k) {
+    const double2 h0 = Hc[k], h1 = Hc[k + 1];
+    // [c s; -conj(s) c] [h0; h1]
+    Hc[k] = cadd(cscale(h0, cs[k]), cmul(sn[k], h1));
+    Hc[k + 1] = csub(cscale(h1, cs[k]), cmulc(sn[k], h0));
+  }
+  const double2 av = Hc[j];
+  const double aa = sqrt(av.x * av.x + av.y * av.y);
+  double cj;
+  double2 sj, rj;
+  if (aa == 0.0) {
+    cj = 0.0;
+    sj = make_double2(1.0, 0.0);
+    rj = make_double2(hn, 0.0);
+  } else {
+    const double t = sqrt(aa * aa + hn * hn);
+    cj = aa / t;
+    const double2 ph = make_double2(av.x / aa, av.y / aa);
+    sj = cscale(ph, hn / t);  // (a/|a|) conj(b)/t with b = hn real
+    rj = cscale(ph, t);
+  }
+  cs[j] = cj;
+  sn[j] = sj;
+  Hc[j] = rj;
+  Hc[j + 1] = make_double2(0.0, 0.0);
+  const double2 g = gam[j];
+  gam[j + 1] = cscale(cmulc(sj, g), -1.0);
+  gam[j] = cscale(g, cj);
+  const double2 gn = gam[j + 1];
+  const double res = sqrt(gn.x * gn.x + gn.y * gn.y);
+  st->res_est = res;
+  st->ncols = j + 1;
+  st->iters += 1;
+  const bool breakdown = !(hn > 1e-30);  // basis vectors have unit norm
+  c.sc[(size_t)b * (m + 1) + j + 1] = breakdown ? 0.0 : 1.0 / hn;
+  if (!isfinite(res) || !isfinite(hn)) {
+    st->nan = 1;
+    st->active = 0;
+  } else if (res <= st->thresh || breakdown || j + 1 >= m || st->iters >= c.max_iters) {
+    st->active = 0;
+  }
+}
+
+__global__ void __launch_bounds__(RED_THREADS) k_update(UpdArgs a) {
+  const int b = blockIdx.y;
+  KState* st = a.ctx.st + b;
+  if (!st->active) return;
+  const int nv = a.j + 1;
+  __shared__ float2 u[65];
+  for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+    const double s = a.ctx.sc[(size_t)b * (a.m + 1) + k];
+    const double2 h = a.ctx.hpass[(size_t)b * (a.m + 1) + k];
+    u[k] = make_float2((float)(s * h.x), (float)(s * h.y));
+  }
+  __syncthreads();
+  float2* w = a.V + ((size_t)(a.j + 1) * a.B + b) * a.n;
+  const unsigned nblk = gridDim.x;
+  const size_t stride = (size_t)nblk * blockDim.x;
+  float nrm = 0.f;
+  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
+    float2 wv = w[n];
+    for (int k = 0; k < nv; ++k) {
+      const float2 v = a.V[((size_t)k * a.B + b) * a.n + n];
+      const float2 c = u[k];
+      wv.x -= v.x * c.x - v.y * c.y;
+      wv.y -= v.x * c.y + v.y * c.x;
+    }
+    w[n] = wv;
+    nrm += wv.x * wv.x + wv.y * wv.y;
+  }
+  if (!a.final_pass) return;
+  __shared__ double sm[32];
+  double acc[1] = {(double)nrm};
+  block_sum<1>(acc, sm);
+  double* part = a.ctx.partial + (size_t)b * a.ctx.part_stride;
+  if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+  if (!last_block(a.ctx.counter + 2 * b + 1, nblk)) return;
+  double s[1] = {0.0};
+  for (unsigned q = threadIdx.x; q < nblk; q += blockDim.x) s[0] += __ldcg(part + q);
+  block_sum<1>(s, sm);
+  if (threadIdx.x == 0) givens_finish(a, b, sqrt(s[0]));
+}
+
+// ------------------------------------------------- triangular solve + update
+__global__ void k_trisolve(KCtx c, int B, int m) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  KState* st = c.st + b;
+  const int k = st->ncols;
+  double2* y = c.y + (size_t)b * m;
+  const double2* gam = c.gam + (size_t)b * (m + 1);
+  for (int r = k - 1; r >= 0; --r) {
+    double2 t = gam[r];
+    for (int q = r + 1; q < k; ++q) {
+      const double2 h = c.H[((size_t)b * m + q) * (m + 1) + r];
+      t = csub(t, cmul(h, y[q]));
+    }
+    const double2 d = c.H[((size_t)b * m + r) * (m + 1) + r];
+    const double dd = d.x * d.x + d.y * d.y;
+    y[r] = dd > 0 ? cscale(cmulc(d, t), 1.0 / dd) : make_double2(0.0, 0.0);
+  }
+}
+
+struct XupArgs {
+  size_t n;
+  int B, m, flexible;
+  const float2* V;  // basis (unscaled)
+  const float2* Z;  // preconditioned basis (flexible)
+  double2* x;
+  double xscale;    // 1/scale: corrections of the non-dimensional system
+  KCtx ctx;
+};
+
+__global__ void __launch_bounds__(RED_THREADS) k_xupdate(XupArgs a) {
+  const int b = blockIdx.y;
+  const KState* st = a.ctx.st + b;
+  const int k = st->ncols;
+  if (k == 0 || st->done) return;
+  __shared__ double2 cy[64];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    double2 yy = a.ctx.y[(size_t)b * a.m + q];
+    if (!a.flexible) yy = cscale(yy, a.ctx.sc[(size_t)b * (a.m + 1) + q]);
+    cy[q] = yy;
+  }
+  __syncthreads();
+  const float2* base = a.flexible ? a.Z : a.V;
+  double2* x = a.x + b * a.n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int q = 0; q < k; ++q) {
+      const float2 v = base[((size_t)q * a.B + b) * a.n + n];
+      acc = cfma(cy[q], to_d(v), acc);
+    }
+    // The cycle solved A' d = r with A' = scale*A and r the residual of
+    // A' x = scale*b, so d is already a correction of x in SI units.
+    x[n] = cadd(x[n], acc);
+  }
+}
+
+__global__ void k_to_f32(const double* in, float* out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+
+__global__ void k_zero_c128(double2* x, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    x[i] = make_double2(0.0, 0.0);
+}
+
+// ----------------------------------------------------------- workspace
+struct Layout {
+  size_t eps32, V, Z, partial, counter, st, H, cs, sn, gam, sc, y, hpass, pc, total;
+  size_t part_stride;
+  int nblk;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int reduction_blocks(size_t n, int B) {
+  const long target = 4L * sm_count();
+  long nb = (target + B - 1) / B;
+  long cap = (long)((n + RED_THREADS * 4 - 1) / (RED_THREADS * 4));
+  return (int)std::max(1L, std::min(nb, cap));
+}
+
+static Layout layout(const cev_fdfd_plan_s* p, const cev_solve_opts& o) {
+  Layout L{};
+  const size_t N = p->n();
+  const int B = p->batch, m = o.restart;
+  dim3 g, bl;
+  int rows;
+  launch_geometry(p->nx, p->ny, B, g, bl, rows);
+  const size_t res_blocks = (size_t)g.x * g.y;
+  L.nblk = reduction_blocks(N, B);
+  L.part_stride = std::max((size_t)L.nblk * 2 * (m + 1), res_blocks * 2);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = off;
+    off = align256(off + bytes);
+    return at;
+  };
+  L.eps32 = take(sizeof(float) * N * B);
+  L.V = take(sizeof(float2) * N * B * (m + 1));
+  L.Z = take(o.precond != CEV_PRECOND_NONE ? sizeof(float2) * N * B * m : 0);
+  L.partial = take(sizeof(double) * L.part_stride * B);
+  L.counter = take(sizeof(unsigned) * 2 * B);
+  L.st = take(sizeof(KState) * B);
+  L.H = take(sizeof(double2) * (size_t)B * m * (m + 1));
+  L.cs = take(sizeof(double) * (size_t)B * m);
+  L.sn = take(sizeof(double2) * (size_t)B * m);
+  L.gam = take(sizeof(double2) * (size_t)B * (m + 1));
+  L.sc = take(sizeof(double) * (size_t)B * (m + 1));
+  L.y = take(sizeof(double2) * (size_t)B * m);
+  L.hpass = take(sizeof(double2) * (size_t)B * (m + 1));
+  L.pc = off;
+  off = align256(off + precond_workspace_size(p, o));
+  L.total = off;
+  return L;
+}
+
+}  // namespace cev
+
+using namespace cev;
+
+extern "C" {
+
+void cev_solve_opts_default(cev_solve_opts* o) {
+  if (!o) return;
+  o->tol = 1e-6;
+  o->inner_rtol = 1e-4;
+  o->max_iters = 20000;
+  o->restart = 30;
+  o->precond = CEV_PRECOND_NONE;
+  o->transpose = 0;
+  o->use_x0 = 0;
+  o->reorth = 0;
+  o->max_stall = 20;
+  o->mg_levels = 0;
+  o->mg_shift = 0.5;
+  o->learned = nullptr;
+}
+
+size_t cev_fdfd_solve_workspace_size(cev_fdfd_plan p, const cev_solve_opts* opts) {
+  if (!p || !opts || opts->restart < 1 || opts->restart > 64) return 0;
+  return layout(p, *opts).total;
+}
+
+int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const void* bvec, void* xvec,
+                   const cev_solve_opts* opts, cev_solve_info* info, void* ws, size_t ws_bytes,
+                   cudaStream_t s) {
+  CEV_REQUIRE(p != nullptr, "plan is NULL");
+  CEV_REQUIRE(opts != nullptr, "opts is NULL");
+  CEV_REQUIRE(eps && bvec && xvec && info, "NULL argument");
+  const cev_solve_opts& o = *opts;
+  CEV_REQUIRE(o.restart >= 1 && o.restart <= 64, "restart must be in [1, 64], got %d", o.restart);
+  CEV_REQUIRE(o.tol > 0 && o.tol < 1, "tol must be in (0, 1)");
+  CEV_REQUIRE(o.max_iters >= 1, "max_iters must be >= 1");
+  CEV_REQUIRE(o.precond == CEV_PRECOND_NONE || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN ||
+                  o.precond == CEV_PRECOND_LEARNED,
+              "unknown preconditioner %d", o.precond);
+  const Layout L = layout(p, o);
+  CEV_REQUIRE(ws != nullptr && ws_bytes >= L.total,
+              "workspace too small: need %zu bytes, got %zu", L.total, ws_bytes);
+  CEV_REQUIRE(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
+
+  const size_t N = p->n();
+  const int B = p->batch, m = o.restart;
+  const int tr = o.transpose ? 1 : 0;
+  char* w = (char*)ws;
+  KCtx c;
+  c.st = (KState*)(w + L.st);
+  c.partial = (double*)(w + L.partial);
+  c.part_stride = L.part_stride;
+  c.counter = (unsigned*)(w + L.counter);
+  c.H = (double2*)(w + L.H);
+  c.cs = (double*)(w + L.cs);
+  c.sn = (double2*)(w + L.sn);
+  c.gam = (double2*)(w + L.gam);
+  c.sc = (double*)(w + L.sc);
+  c.y = (double2*)(w + L.y);
+  c.hpass = (double2*)(w + L.hpass);
+  c.tol = o.tol;
+  c.inner_rtol = o.inner_rtol;
+  c.max_iters = o.max_iters;
+  float* eps32 = (float*)(w + L.eps32);
+  float2* V = (float2*)(w + L.V);
+  float2* Z = (float2*)(w + L.Z);
+  const bool flexible = o.precond != CEV_PRECOND_NONE;
+
+  CEV_CUDA(cudaMemsetAsync(c.counter, 0, sizeof(unsigned) * 2 * B, s));
+  CEV_CUDA(cudaMemsetAsync(c.st, 0, sizeof(KState) * B, s));
+  const size_t ne = eps_shared ? N : N * B;
+  k_to_f32<<<std::min(ceil_div(ne, 256), 8u * sm_count()), 256, 0, s>>>(eps, eps32, ne);
+  if (!o.use_x0)
+    k_zero_c128<<<std::min(ceil_div(N * B, 256), 8u * sm_count()), 256, 0, s>>>((double2*)xvec,
+                                                                               N * B);
+  CEV_CHECK_LAUNCH("solve init");
+
+  Precond pc;
+  int rc = precond_setup(pc, p, o, eps32, eps_shared, w + L.pc, s);
+  if (rc != CEV_OK) return rc;
+
+  dim3 sg, sb;
+  int rows;
+  launch_geometry(p->nx, p->ny, B, sg, sb, rows);
+  const dim3 rg(L.nblk, B, 1);
+
+  auto residual = [&](int first) -> int {
+    if (p->pol == POL_EZ) {
+      ResArgs<POL_EZ> a{p->nx, p->ny, rows, first, m, eps, eps_shared ? 0 : N,
+                        (const double2*)xvec, (const double2*)bvec, p->scale,
+                        p->cx64[tr], p->cy64[tr], p->k2_64, V, N, c};
+      k_residual<POL_EZ><<<sg, sb, 0, s>>>(a);
+    } else {
+      ResArgs<POL_HZ> a{p->nx, p->ny, rows, first, m, eps, eps_shared ? 0 : N,
+                        (const double2*)xvec, (const double2*)bvec, p->scale,
+                        p->cx64[tr], p->cy64[tr], p->k2_64, V, N, c};
+      k_residual<POL_HZ><<<sg, sb, 0, s>>>(a);
+    }
+    CEV_CHECK_LAUNCH("k_residual");
+    return CEV_OK;
+  };
+  auto matvec = [&](int j, const float2* in, size_t in_bs, int use_scale) -> int {
+    float2* out = V + (size_t)(j + 1) * B * N;
+    if (p->pol == POL_EZ) {
+      MvArgs<POL_EZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, in_bs, use_scale,
+                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
+      k_arnoldi_mv<POL_EZ><<<sg, sb, 0, s>>>(a);
+    } else {
+      MvArgs<POL_HZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, in_bs, use_scale,
+                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
+      k_arnoldi_mv<POL_HZ><<<sg, sb, 0, s>>>(a);
+    }
+    CEV_CHECK_LAUNCH("k_arnoldi_mv");
+    return CEV_OK;
+  };
+
+  std::vector<KState> hst(B);
+  std::vector<double> best(B, INFINITY);
+  std::vector<int> stall(B, 0), status(B, CEV_NOT_CONVERGED), cycles(B, 0);
+  if ((rc = residual(1)) != CEV_OK) return rc;
+  int total_iters = 0;
+  for (int cyc = 0;; ++cyc) {
+    CEV_CUDA(cudaMemcpyAsync(hst.data(), c.st, sizeof(KState) * B, cudaMemcpyDeviceToHost, s));
+    CEV_CUDA(cudaStreamSynchronize(s));
+    bool any = false, changed = false;
+    for (int b = 0; b < B; ++b) {
+      KState& q = hst[b];
+      if (q.done) continue;
+      cycles[b] = cyc;
+      const double rel = q.bnorm > 0 ? q.beta / q.bnorm : 0.0;
+      int stt = -100;
+      if (q.nan || !std::isfinite(rel)) stt = CEV_ERR_NUMERIC;
+      else if (q.bnorm == 0 || rel <= o.tol) stt = CEV_OK;
+      else if (q.iters >= o.max_iters) stt = CEV_NOT_CONVERGED;
+      else {
+        if (rel < 0.9 * best[b]) {
+          best[b] = rel;
+          stall[b] = 0;
+        } else if (++stall[b] > o.max_stall) {
+          stt = CEV_STAGNATED;
+        }
+      }
+      if (stt != -100) {
+        status[b] = stt;
+        q.done = 1;
+        q.active = 0;
+        changed = true;
+      } else {
+        any = true;
+      }
+    }
+    if (changed) CEV_CUDA(cudaMemcpyAsync(c.st, hst.data(), sizeof(KState) * B,
+                                          cudaMemcpyHostToDevice, s));
+    if (!any) break;
+    for (int j = 0; j < m; ++j) {
+      const float2* vin = V + (size_t)j * B * N;
+      if (flexible) {
+        float2* zj = Z + (size_t)j * B * N;
+        if ((rc = precond_apply(pc, c, j, m, vin, zj, s)) != CEV_OK) return rc;
+        if ((rc = matvec(j, zj, N, 0)) != CEV_OK) return rc;
+      } else {
+        if ((rc = matvec(j, vin, N, 1)) != CEV_OK) return rc;
+      }
+      for (int pass = 0; pass < (o.reorth ? 2 : 1); ++pass) {
+        const bool final_pass = pass == (o.reorth ? 1 : 0);
+        DotArgs da{N, B, m, j, pass, V, c};
+        k_multidot<<<rg, RED_THREADS, 0, s>>>(da);
+        UpdArgs ua{N, B, m, j, final_pass ? 1 : 0, V, c};
+        k_update<<<rg, RED_THREADS, 0, s>>>(ua);
+      }
+      CEV_CHECK_LAUNCH("arnoldi step");
+    }
+    total_iters += m;
+    k_trisolve<<<(B + 63) / 64, 64, 0, s>>>(c, B, m);
+    XupArgs xa{N, B, m, flexible ? 1 : 0, V, Z, (double2*)xvec, 1.0, c};
+    k_xupdate<<<rg, RED_THREADS, 0, s>>>(xa);
+    CEV_CHECK_LAUNCH("cycle finish");
+    if ((rc = residual(0)) != CEV_OK) return rc;
+  }
+  int worst = CEV_OK;
+  for (int b = 0; b < B; ++b) {
+    info[b].status = status[b];
+    info[b].iterations = hst[b].iters;
+    info[b].cycles = cycles[b];
+    info[b].reserved = 0;
+    info[b].bnorm = hst[b].bnorm / p->scale;
+    info[b].residual = hst[b].bnorm > 0 ? hst[b].beta / hst[b].bnorm : 0.0;
+    if (status[b] < 0) worst = std::min(worst, status[b]);
+    else if (worst >= 0) worst = std::max(worst, status[b]);
+  }
+  return worst;
+}
+
+}  // extern "C"

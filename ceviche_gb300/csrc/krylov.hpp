@@ -1,0 +1,51 @@
+// Krylov solver state shared by the solver and the preconditioners.
+#pragma once
+
+#include "fdfd_plan.hpp"
+
+namespace cev {
+
+// Per-problem scalars of the batched GMRES, finalised on the device.
+struct KState {
+  double bnorm;    // ||b'|| of the non-dimensional system
+  double beta;     // FP64 true residual norm at the start of the cycle
+  double res_est;  // Givens estimate of the current residual norm
+  double thresh;   // cycle stops when res_est <= thresh
+  int active;      // Arnoldi work enabled for this problem
+  int ncols;       // Krylov columns accumulated in the cycle
+  int iters;       // total Arnoldi iterations
+  int nan;         // non-finite value seen
+  int done;        // host decided the problem is finished
+  int pad[3];
+};
+
+// Device pointers of the solver workspace.
+struct KCtx {
+  KState* st;
+  double* partial;      // [B][part_stride] cross-block partial sums
+  size_t part_stride;
+  unsigned* counter;    // [B][2] arrival counters (self-resetting)
+  double2* H;           // [B][m][m+1] Hessenberg columns (rotated into R)
+  double* cs;           // [B][m] Givens cosines
+  double2* sn;          // [B][m] Givens sines
+  double2* gam;         // [B][m+1] rotated residual vector
+  double* sc;           // [B][m+1] 1/||v_k|| (basis stored unnormalised)
+  double2* y;           // [B][m] least-squares solution
+  double2* hpass;       // [B][m+1] projections of the current pass
+  double tol, inner_rtol;
+  int max_iters;
+};
+
+// Right preconditioner used by flexible GMRES: z = M^{-1} (sc_j v_j).
+struct Precond {
+  int kind = CEV_PRECOND_NONE;
+  void* impl = nullptr;
+};
+
+size_t precond_workspace_size(const cev_fdfd_plan_s* p, const cev_solve_opts& o);
+int precond_setup(Precond& pc, const cev_fdfd_plan_s* p, const cev_solve_opts& o, const float* eps32,
+                  int eps_shared, void* ws, cudaStream_t s);
+int precond_apply(Precond& pc, const KCtx& c, int j, int m, const float2* v, float2* z,
+                  cudaStream_t s);
+
+}  // namespace cev

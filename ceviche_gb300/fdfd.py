@@ -1,0 +1,122 @@
+"""Drop-in ``fdfd_ez`` / ``fdfd_hz`` (ceviche/fdfd.py:11-244) on the GPU.
+
+Same constructor, ``eps_r`` setter and ``solve(source) -> (F1, F2, Fz)``
+contract.  numpy inputs give numpy complex128 outputs; torch inputs give
+device tensors that are differentiable with respect to ``eps_r`` and the
+source (reverse mode through the transposed GPU solve).
+
+Extensions: ``omega`` may be a 1D array (a batch of frequencies solved
+together) and ``eps_r``/``source`` may carry a leading batch dimension;
+solver options (``tol``, ``restart``, ``precond``, ...) are keyword arguments.
+"""
+import numpy as np
+import torch
+
+from . import primitives as prim
+
+
+def _to_tensor(a, dtype):
+    if torch.is_tensor(a):
+        t = a
+        if not t.is_cuda:
+            t = t.cuda()
+        return t.to(dtype) if t.dtype != dtype else t
+    return torch.as_tensor(np.asarray(a), dtype=dtype, device="cuda")
+
+
+class fdfd:
+    """Base class (ceviche/fdfd.py:11-162)."""
+
+    pol = None
+
+    def __init__(self, omega, dL, eps_r, npml, bloch_phases=None, **solver_opts):
+        self.omega = omega
+        self.dL = dL
+        self.npml = npml
+        self._setup_bloch_phases(bloch_phases)
+        self.eps_r = eps_r
+        self.solver_opts = dict(solver_opts)
+        self.last_info = None
+
+    # -- eps_r property (fdfd.py:35-44)
+    @property
+    def eps_r(self):
+        return self._eps_r
+
+    @eps_r.setter
+    def eps_r(self, new_eps):
+        self._save_shape(new_eps)
+        self._eps_r = new_eps
+
+    def _save_shape(self, grid):
+        shape = tuple(grid.shape)
+        if len(shape) not in (2, 3):
+            raise ValueError(f"eps_r must be (Nx, Ny) or (batch, Nx, Ny), got {shape}")
+        self.shape = shape[-2:]
+        self.Nx, self.Ny = self.shape
+        self.N = self.Nx * self.Ny
+
+    def _setup_bloch_phases(self, bloch_phases):
+        """ceviche/fdfd.py:101-112."""
+        self.bloch_x = 0.0
+        self.bloch_y = 0.0
+        self.bloch_z = 0.0
+        if bloch_phases is not None:
+            self.bloch_x = bloch_phases[0]
+            if len(bloch_phases) > 1:
+                self.bloch_y = bloch_phases[1]
+            if len(bloch_phases) > 2:
+                self.bloch_z = bloch_phases[2]
+
+    def _vec_to_grid(self, vec):
+        return vec.reshape(self.shape)
+
+    def _grid_to_vec(self, grid):
+        return grid.flatten()
+
+    # -- plan / operator access
+    def _plan(self):
+        return prim.get_plan(self.pol, self.shape, self.dL, self.omega, self.npml,
+                             (self.bloch_x, self.bloch_y))
+
+    def A(self, x, transpose=False):
+        """Matrix-free system matrix product A x (SI units), x of grid shape."""
+        eps = _to_tensor(self.eps_r, torch.float64)
+        xt = _to_tensor(x, torch.complex128)
+        y = prim.apply(self._plan(), eps, xt, transpose=transpose)
+        return y.reshape(xt.shape)
+
+    def solve(self, source_z):
+        """Solve for the fields of this polarisation (ceviche/fdfd.py:58-76)."""
+        if np.iscomplexobj(self.eps_r) if not torch.is_tensor(self.eps_r) \
+                else self.eps_r.is_complex():
+            raise NotImplementedError("complex eps_r is not supported by the GPU solver yet")
+        numpy_out = not torch.is_tensor(self.eps_r) and not torch.is_tensor(source_z)
+        eps = _to_tensor(self.eps_r, torch.float64)
+        src = source_z if torch.is_tensor(source_z) else np.asarray(source_z)
+        src_dtype = torch.complex128 if (torch.is_tensor(src) and src.is_complex()) or \
+            (not torch.is_tensor(src) and np.iscomplexobj(src)) else torch.float64
+        src = _to_tensor(src, src_dtype)
+        plan = self._plan()
+        f1, f2, fz = prim.FDFDSolve.apply(eps, src, plan, self.solver_opts)
+        self.last_info = getattr(prim, "_last_info", None)
+        squeeze = np.ndim(self.omega) == 0 and eps.dim() == 2 and src.dim() == 2
+        out = []
+        for f in (f1, f2, fz):
+            f = f[0] if squeeze else f
+            out.append(f.detach().cpu().numpy() if numpy_out else f)
+        return tuple(out)
+
+
+class fdfd_ez(fdfd):
+    """Ez polarisation: A = -(1/mu0)(Dxf Dxb + Dyf Dyb) - eps0 w^2 eps
+    (ceviche/fdfd.py:166-192).  solve(Jz) -> (Hx, Hy, Ez)."""
+
+    pol = "ez"
+
+
+class fdfd_hz(fdfd):
+    """Hz polarisation: A = (1/eps0)(Dxb/eps_yy Dxf + Dyb/eps_xx Dyf) + mu0 w^2
+    (ceviche/fdfd.py:194-244).  solve(Mz) -> (Ex, Ey, Hz)."""
+
+    pol = "hz"

@@ -1,0 +1,277 @@
+"""Device-side FDFD primitives over the C ABI, and their autograd rules.
+
+Replaces ceviche/primitives.py: ``sp_mult`` (the matrix-free operator
+``apply``), ``sp_solve`` (``solve``, a GPU Krylov solve instead of the sparse
+LU of ceviche/solvers.py:50-62) and their reverse/forward derivatives
+(primitives.py:74-148), specialised to the Yee system matrices so no sparse
+entries/indices ever exist.
+
+Gradient convention: PyTorch's (g = dL/dRe + i dL/dIm).  For a real loss and
+real eps the gradients equal ceviche/HIPS-autograd's.
+"""
+import ctypes as C
+import warnings
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, ptr, stream_ptr
+from .constants import EPSILON_0, MU_0
+
+_DEFAULT_OPTS = dict(tol=1e-6, inner_rtol=1e-4, max_iters=20000, restart=30, precond="none",
+                     reorth=0, max_stall=20, mg_levels=0, mg_shift=0.5)
+
+
+class SolverWarning(UserWarning):
+    """A solve finished without reaching its tolerance."""
+
+
+def _require_cuda():
+    if not torch.cuda.is_available():
+        raise _lib.CevError("ceviche_gb300 needs a CUDA device (sm_103a); none is available")
+
+
+class Plan:
+    """Owns a cev_fdfd_plan: PML stencil tables for a batch of omegas on one grid."""
+
+    def __init__(self, pol, shape, dL, omegas, npml, bloch=(0.0, 0.0)):
+        _require_cuda()
+        lib = _lib.load()
+        self.pol = {"ez": _lib.POL_EZ, "hz": _lib.POL_HZ}[pol]
+        self.pol_name = pol
+        self.nx, self.ny = int(shape[0]), int(shape[1])
+        self.omegas = np.atleast_1d(np.asarray(omegas, dtype=np.float64)).copy()
+        self.batch = len(self.omegas)
+        self.dL = float(dL)
+        self.npml = (int(npml[0]), int(npml[1]))
+        self.bloch = (float(bloch[0]), float(bloch[1]))
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        h = C.c_void_p()
+        om = self.omegas.ctypes.data_as(C.POINTER(C.c_double))
+        check(lib.cev_fdfd_plan_create(C.byref(h), self.pol, self.nx, self.ny, self.batch,
+                                       self.dL, om, self.npml[0], self.npml[1],
+                                       self.bloch[0], self.bloch[1]), "plan_create")
+        self.handle = h
+        self.scale = lib.cev_fdfd_plan_scale(h)
+        self.omega_t = torch.tensor(self.omegas, dtype=torch.float64, device=self.device)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.cev_fdfd_plan_destroy(h)
+            self.handle = None
+
+    @property
+    def shape(self):
+        return (self.nx, self.ny)
+
+
+_plan_cache = {}
+
+
+def get_plan(pol, shape, dL, omegas, npml, bloch=(0.0, 0.0)):
+    om = tuple(float(w) for w in np.atleast_1d(omegas))
+    key = (pol, int(shape[0]), int(shape[1]), float(dL), om, int(npml[0]), int(npml[1]),
+           float(bloch[0]), float(bloch[1]), torch.cuda.current_device())
+    p = _plan_cache.get(key)
+    if p is None:
+        if len(_plan_cache) > 64:
+            _plan_cache.clear()
+        p = _plan_cache[key] = Plan(pol, shape, dL, om, npml, bloch)
+    return p
+
+
+def _eps_arg(plan, eps, dtype):
+    """eps as a contiguous (1 or batch, nx, ny) device tensor; returns (eps, shared)."""
+    e = eps.to(device=plan.device, dtype=dtype).contiguous()
+    if e.dim() == 2:
+        e = e.unsqueeze(0)
+    if e.shape[-2:] != (plan.nx, plan.ny):
+        raise ValueError(f"eps shape {tuple(e.shape)} does not match grid {plan.shape}")
+    if e.shape[0] not in (1, plan.batch):
+        raise ValueError(f"eps batch {e.shape[0]} must be 1 or {plan.batch}")
+    return e, int(e.shape[0] == 1 and plan.batch >= 1)
+
+
+def _field_arg(plan, x, dtype):
+    t = x.to(device=plan.device, dtype=dtype)
+    if t.dim() == 2:
+        t = t.unsqueeze(0)
+    if t.shape != (plan.batch, plan.nx, plan.ny):
+        if t.shape[0] == 1 and plan.batch > 1:
+            t = t.expand(plan.batch, plan.nx, plan.ny)
+        else:
+            raise ValueError(f"field shape {tuple(t.shape)} does not match "
+                             f"({plan.batch}, {plan.nx}, {plan.ny})")
+    return t.contiguous()
+
+
+def apply(plan, eps, x, transpose=False, precision="c128", si_units=True):
+    """y = A x (or A^T x) on the GPU; x complex (batch, nx, ny)."""
+    lib = _lib.load()
+    if precision == "c128":
+        e, sh = _eps_arg(plan, eps, torch.float64)
+        xt = _field_arg(plan, x, torch.complex128)
+        prec = _lib.PREC_C128
+    else:
+        e, sh = _eps_arg(plan, eps, torch.float32)
+        xt = _field_arg(plan, x, torch.complex64)
+        prec = _lib.PREC_C64
+    y = torch.empty_like(xt)
+    check(lib.cev_fdfd_apply(plan.handle, ptr(e), sh, ptr(xt), ptr(y), int(bool(transpose)), prec,
+                             int(bool(si_units)), stream_ptr()), "apply")
+    return y
+
+
+def make_opts(**kw):
+    o = dict(_DEFAULT_OPTS)
+    for k, v in kw.items():
+        if v is None:
+            continue
+        if k not in o and k not in ("transpose", "use_x0", "learned"):
+            raise TypeError(f"unknown solver option {k!r}")
+        o[k] = v
+    s = _lib.SolveOpts()
+    _lib.load().cev_solve_opts_default(C.byref(s))
+    s.tol = float(o["tol"])
+    s.inner_rtol = float(o["inner_rtol"])
+    s.max_iters = int(o["max_iters"])
+    s.restart = int(o["restart"])
+    s.precond = _lib.PRECOND[o["precond"]] if isinstance(o["precond"], str) else int(o["precond"])
+    s.transpose = int(bool(o.get("transpose", 0)))
+    s.use_x0 = int(bool(o.get("use_x0", 0)))
+    s.reorth = int(o["reorth"])
+    s.max_stall = int(o["max_stall"])
+    s.mg_levels = int(o["mg_levels"])
+    s.mg_shift = float(o["mg_shift"])
+    lp = o.get("learned")
+    s.learned = None if lp is None else C.c_void_p(lp.handle_ptr())
+    return s
+
+
+def _workspace(nbytes, device):
+    buf = torch.empty(nbytes + 256, dtype=torch.uint8, device=device)
+    off = (-buf.data_ptr()) % 256
+    return buf, buf.data_ptr() + off
+
+
+class SolveResult(list):
+    """Per-problem solve records (status, iterations, cycles, residual)."""
+
+
+def solve(plan, eps, b, transpose=False, x0=None, strict=False, **opts):
+    """Solve A x = b (A^T x = b) for every problem; b complex (batch, nx, ny) in SI units.
+
+    Returns (x complex128, infos).  Non-convergence warns (or raises with strict).
+    """
+    lib = _lib.load()
+    e, sh = _eps_arg(plan, eps, torch.float64)
+    bt = _field_arg(plan, b, torch.complex128)
+    s = make_opts(transpose=transpose, use_x0=x0 is not None, **opts)
+    if x0 is not None:
+        x = _field_arg(plan, x0, torch.complex128).clone()
+    else:
+        x = torch.empty_like(bt)
+    nbytes = lib.cev_fdfd_solve_workspace_size(plan.handle, C.byref(s))
+    if nbytes == 0:
+        raise ValueError("invalid solver options")
+    ws, wptr = _workspace(nbytes, plan.device)
+    infos = (_lib.SolveInfo * plan.batch)()
+    rc = lib.cev_fdfd_solve(plan.handle, ptr(e), sh, ptr(bt), ptr(x), C.byref(s), infos,
+                            C.c_void_p(wptr), nbytes, stream_ptr())
+    check(rc, "solve")
+    res = SolveResult(dict(status=_lib.STATUS_NAMES.get(i.status, i.status), code=i.status,
+                           iterations=i.iterations, cycles=i.cycles, residual=i.residual)
+                      for i in infos)
+    del ws
+    if rc > 0:
+        msg = (f"FDFD solve did not reach tol={s.tol:g}: "
+               + ", ".join(f"[{k}] {r['status']} res={r['residual']:.3g} it={r['iterations']}"
+                           for k, r in enumerate(res) if r["code"] != 0))
+        if strict:
+            raise _lib.CevError(msg)
+        warnings.warn(msg, SolverWarning, stacklevel=2)
+    return x, res
+
+
+def fields(plan, eps, fz):
+    """Secondary field components (f1, f2) from the solved component (SI, complex128)."""
+    lib = _lib.load()
+    e, sh = _eps_arg(plan, eps, torch.float64)
+    z = _field_arg(plan, fz, torch.complex128)
+    f1 = torch.empty_like(z)
+    f2 = torch.empty_like(z)
+    check(lib.cev_fdfd_fields(plan.handle, ptr(e), sh, ptr(z), ptr(f1), ptr(f2), stream_ptr()),
+          "fields")
+    return f1, f2
+
+
+def fields_adjoint(plan, eps, fz, g1, g2, gz, geps):
+    """gz += M1^H g1 + M2^H g2 (in place); geps += direct eps term (Hz)."""
+    lib = _lib.load()
+    e, sh = _eps_arg(plan, eps, torch.float64)
+    z = _field_arg(plan, fz, torch.complex128)
+    a = _field_arg(plan, g1, torch.complex128)
+    b = _field_arg(plan, g2, torch.complex128)
+    check(lib.cev_fdfd_fields_adjoint(plan.handle, ptr(e), sh, ptr(z), ptr(a), ptr(b), ptr(gz),
+                                      ptr(geps), stream_ptr()), "fields_adjoint")
+
+
+def grad_eps(plan, eps, x, mu, geps):
+    """geps += system-matrix part of dL/d(eps) given x and mu = A^-T conj(g_x)."""
+    lib = _lib.load()
+    e, sh = _eps_arg(plan, eps, torch.float64)
+    xt = _field_arg(plan, x, torch.complex128)
+    m = _field_arg(plan, mu, torch.complex128)
+    check(lib.cev_fdfd_grad_eps(plan.handle, ptr(e), sh, ptr(xt), ptr(m), ptr(geps), stream_ptr()),
+          "grad_eps")
+
+
+class FDFDSolve(torch.autograd.Function):
+    """(eps, src) -> (F1, F2, Fz) of ceviche's fdfd.solve with b = 1j*omega*src.
+
+    Backward: the transposed GPU solve of primitives.py:121-135 plus the eps
+    chain of fdfd.py:179 (Ez) / 211-233 (Hz) and of the field conversions.
+    """
+
+    @staticmethod
+    def forward(ctx, eps, src, plan, opts):
+        om = plan.omega_t.view(-1, 1, 1)
+        s = _field_arg(plan, src, torch.complex128)
+        b = 1j * om * s
+        x, info = solve(plan, eps, b, **opts)
+        f1, f2 = fields(plan, eps, x)
+        ctx.plan, ctx.opts = plan, opts
+        ctx.src_real = not src.is_complex()
+        ctx.src_shape = src.shape
+        ctx.eps_shape = eps.shape
+        ctx.save_for_backward(eps, x)
+        ctx.info = info
+        return f1, f2, x
+
+    @staticmethod
+    def backward(ctx, g1, g2, gz):
+        plan = ctx.plan
+        eps, x = ctx.saved_tensors
+        e, sh = _eps_arg(plan, eps, torch.float64)
+        zeros = lambda: torch.zeros_like(x)
+        g1 = zeros() if g1 is None else g1.to(torch.complex128).contiguous()
+        g2 = zeros() if g2 is None else g2.to(torch.complex128).contiguous()
+        gx = zeros() if gz is None else gz.to(torch.complex128).contiguous().clone()
+        geps = torch.zeros_like(e)
+        fields_adjoint(plan, e, x, g1, g2, gx, geps if plan.pol_name == "hz" else None)
+        geps_out = grad_src = None
+        mu, _ = solve(plan, e, gx.conj().resolve_conj(), transpose=True, **ctx.opts)
+        if ctx.needs_input_grad[0]:
+            grad_eps(plan, e, x, mu, geps)
+            geps_out = geps.reshape(ctx.eps_shape) if geps.numel() == int(np.prod(ctx.eps_shape)) \
+                else geps
+        if ctx.needs_input_grad[1]:
+            lam = mu.conj()
+            gs = -1j * plan.omega_t.view(-1, 1, 1) * lam
+            if len(ctx.src_shape) == 2:
+                gs = gs.sum(0)
+            grad_src = gs.real if ctx.src_real else gs
+            grad_src = grad_src.reshape(ctx.src_shape)
+        return geps_out, grad_src, None, None

@@ -1,0 +1,249 @@
+/*
+ * cevgpu.h -- C ABI of the GB300 (sm_103a) Yee-stencil library that replaces
+ * ceviche's CPU FDFD solve and FDTD time loop.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: CEV_OK (0), < 0 error,
+ *     > 0 "finished but not converged"-style outcomes.  cev_last_error_string()
+ *     describes the last error of the calling thread.
+ *   - Grids are (nx, ny) in C order, flat index i*ny + j (ceviche's
+ *     _grid_to_vec, ceviche/fdfd.py:118-120).  A batch of problems is laid out
+ *     [batch][nx][ny].
+ *   - Complex arrays are interleaved (re, im): complex64 = float2,
+ *     complex128 = double2.
+ *   - All array arguments are DEVICE pointers unless stated otherwise; the
+ *     caller owns them.  Plans own only their small coefficient tables.
+ *   - Work is enqueued on the given stream; host-side validation errors come
+ *     back synchronously.  cev_fdfd_solve synchronises the stream once per
+ *     restart cycle to read the FP64 true residual.
+ */
+#ifndef CEVGPU_H_
+#define CEVGPU_H_
+
+#include <stddef.h>
+#include <cuda_runtime.h>
+
+#if defined(__GNUC__)
+#define CEV_API __attribute__((visibility("default")))
+#else
+#define CEV_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CEV_OK 0
+#define CEV_ERR_INVALID (-1)
+#define CEV_ERR_CUDA (-2)
+#define CEV_ERR_WORKSPACE (-3)
+#define CEV_ERR_NUMERIC (-4)
+#define CEV_NOT_CONVERGED 1
+#define CEV_STAGNATED 2
+
+#define CEV_POL_EZ 0
+#define CEV_POL_HZ 1
+
+#define CEV_PREC_C64 0  /* complex64 fields, float eps   */
+#define CEV_PREC_C128 1 /* complex128 fields, double eps */
+
+#define CEV_PRECOND_NONE 0
+#define CEV_PRECOND_SHIFTED_LAPLACIAN 1
+#define CEV_PRECOND_LEARNED 2
+
+/* Last error message of the calling thread ("" if none). */
+CEV_API const char* cev_last_error_string(void);
+/* Library version, major*10000 + minor*100 + patch. */
+CEV_API int cev_version(void);
+
+/* ============================== FDFD ==================================== */
+
+typedef struct cev_fdfd_plan_s* cev_fdfd_plan;
+
+/*
+ * Precomputes the SC-PML stencil coefficient tables of `batch` problems that
+ * share a grid and differ in omega.  Replaces the per-solve sparse assembly of
+ * ceviche/derivatives.py:44-226 (compute_derivative_matrices, create_S_matrices,
+ * create_sfactor, s_value) and ceviche/fdfd.py:80-112 (_setup_derivatives,
+ * Bloch phases).  omegas is a HOST array of length batch.
+ */
+CEV_API int cev_fdfd_plan_create(cev_fdfd_plan* plan, int pol, int nx, int ny, int batch, double dL,
+                         const double* omegas, int npml_x, int npml_y, double bloch_x,
+                         double bloch_y);
+CEV_API int cev_fdfd_plan_destroy(cev_fdfd_plan plan);
+/* Row scaling of the non-dimensional system the solver works on:
+ * A' = scale*A with scale = mu0*dL^2 (Ez) or eps0*dL^2 (Hz). */
+CEV_API double cev_fdfd_plan_scale(cev_fdfd_plan plan);
+
+/*
+ * y = A x  (transpose=1: y = A^T x) for every problem of the batch.
+ * Matrix-free form of fdfd_ez._make_A / fdfd_hz._make_A
+ * (ceviche/fdfd.py:172-185, 211-233) as applied by sp_mult
+ * (ceviche/primitives.py:58-72); the transpose replaces the transposed-index
+ * products of primitives.py:81-86, 121-135.
+ * precision CEV_PREC_C64: eps is float*, x/y complex64;
+ * CEV_PREC_C128: eps is double*, x/y complex128.
+ * eps_shared=1: one eps grid for the whole batch, else [batch][nx][ny].
+ * si_units=1 returns A x in SI units, 0 the non-dimensional A' x.
+ */
+CEV_API int cev_fdfd_apply(cev_fdfd_plan plan, const void* eps, int eps_shared, const void* x, void* y,
+                   int transpose, int precision, int si_units, cudaStream_t stream);
+
+typedef struct {
+  double tol;         /* target FP64 true relative residual ||Ax-b||/||b|| (default 1e-6) */
+  double inner_rtol;  /* residual reduction at which a complex64 inner cycle stops (1e-4) */
+  int max_iters;      /* cap on Arnoldi iterations over all cycles */
+  int restart;        /* Krylov dimension per cycle, 1..64 */
+  int precond;        /* CEV_PRECOND_* */
+  int transpose;      /* solve A^T x = b (adjoint solve) */
+  int use_x0;         /* x holds an initial guess on entry */
+  int reorth;         /* 1: classical Gram-Schmidt with a second pass */
+  int max_stall;      /* cycles without a 10% residual drop before CEV_STAGNATED */
+  int mg_levels;      /* shifted-Laplacian preconditioner: multigrid levels (0 = auto) */
+  double mg_shift;    /* shifted-Laplacian imaginary shift beta (default 0.5) */
+  const void* learned; /* CEV_PRECOND_LEARNED: a cev_learned_precond handle */
+} cev_solve_opts;
+
+typedef struct {
+  int status;      /* CEV_OK, CEV_NOT_CONVERGED, CEV_STAGNATED, CEV_ERR_NUMERIC */
+  int iterations;  /* Arnoldi iterations spent on this problem */
+  int cycles;      /* restart cycles (= FP64 residual evaluations - 1) */
+  int reserved;
+  double residual; /* final FP64 true relative residual */
+  double bnorm;    /* ||b|| (SI) */
+} cev_solve_info;
+
+/* Fills opts with the defaults documented above. */
+CEV_API void cev_solve_opts_default(cev_solve_opts* opts);
+
+/* Bytes of device workspace cev_fdfd_solve needs for these options. */
+CEV_API size_t cev_fdfd_solve_workspace_size(cev_fdfd_plan plan, const cev_solve_opts* opts);
+
+/*
+ * Solves A x = b (or A^T x = b) for every problem of the batch to the FP64
+ * true relative residual opts->tol with restarted (flexible) GMRES: complex64
+ * Arnoldi cycles on the GPU, each restart an FP64 residual b - A x and an FP64
+ * update of x (mixed-precision iterative refinement).  Replaces
+ * ceviche/primitives.py:103-119 sp_solve -> ceviche/solvers.py:37-62
+ * solve_linear/_solve_direct (and fills the _solve_cuda stub, solvers.py:77-79).
+ * eps: double [1 or batch][nx][ny]; b, x: complex128 [batch][nx][ny] in SI
+ * units (b = 1j*omega*J as built by fdfd.py:189, 237).
+ * info: HOST array of `batch` records.  Returns the worst per-problem status.
+ */
+CEV_API int cev_fdfd_solve(cev_fdfd_plan plan, const double* eps, int eps_shared, const void* b, void* x,
+                   const cev_solve_opts* opts, cev_solve_info* info, void* workspace,
+                   size_t workspace_bytes, cudaStream_t stream);
+
+/*
+ * Secondary fields from the solved component, complex128, SI units.
+ * Ez: (f1, f2) = (Hx, Hy) = (-Dyb Ez, Dxb Ez)/(1j*omega*mu0)   (fdfd.py:138-147)
+ * Hz: (f1, f2) = (Ex, Ey) = (Dyf Hz/(eps_xx+1e-5), -Dxf Hz/(eps_yy+1e-5))/(1j*omega*eps0)
+ *     (fdfd.py:150-162, averages of fdfd.py:200-209)
+ */
+CEV_API int cev_fdfd_fields(cev_fdfd_plan plan, const double* eps, int eps_shared, const void* fz,
+                    void* f1, void* f2, cudaStream_t stream);
+
+/*
+ * Reverse mode of cev_fdfd_fields (PyTorch cotangent convention,
+ * g = dL/dRe + i dL/dIm): gz += M1^H g1 + M2^H g2.  For Hz the direct
+ * dependence of (Ex, Ey) on eps is added to geps (double, same batch layout as
+ * eps; summed over the batch when eps_shared).  Restates the sp_mult x-VJP
+ * (ceviche/primitives.py:81-86) used through fdfd.py:138-162.
+ */
+CEV_API int cev_fdfd_fields_adjoint(cev_fdfd_plan plan, const double* eps, int eps_shared, const void* fz,
+                            const void* g1, const void* g2, void* gz, double* geps,
+                            cudaStream_t stream);
+
+/*
+ * geps += dL/d(eps) contributed by the system matrix, given the forward
+ * solution x and mu = A^{-T} conj(g_x) (the transposed solve of the cotangent).
+ * Ez: Re(mu * eps0*omega^2 * x); Hz: chain through 1/(eps_yy+1e-5),
+ * 1/(eps_xx+1e-5) and the averages.  Restates grad_sp_solve_entries_reverse
+ * (ceviche/primitives.py:121-128) chained to eps by fdfd.py:179 / 211-233.
+ */
+CEV_API int cev_fdfd_grad_eps(cev_fdfd_plan plan, const double* eps, int eps_shared, const void* x,
+                      const void* mu, double* geps, cudaStream_t stream);
+
+/* ============================== FDTD ==================================== */
+
+typedef struct cev_fdtd_plan_s* cev_fdtd_plan;
+
+/*
+ * 2D (Nz = 1) Yee FDTD with ceviche's integrated-sigma PML.
+ * Replaces ceviche/fdtd.py:12-72 (construction, setters), 213-316 (dt,
+ * sigmas, update coefficients).  precision: CEV_PREC_C64 -> float32 fields,
+ * CEV_PREC_C128 -> float64 fields.  eps: DEVICE double [nx][ny].
+ */
+CEV_API int cev_fdtd_plan_create(cev_fdtd_plan* plan, int nx, int ny, double dL, int npml_x, int npml_y,
+                         int precision, const double* eps, cudaStream_t stream);
+CEV_API int cev_fdtd_plan_destroy(cev_fdtd_plan plan);
+/* Replaces the eps_r setter's coefficient refresh (fdtd.py:63-72). */
+CEV_API int cev_fdtd_set_eps(cev_fdtd_plan plan, const double* eps, cudaStream_t stream);
+/* dt of fdtd.py:213-222. */
+CEV_API double cev_fdtd_dt(cev_fdtd_plan plan);
+
+/*
+ * Caller-owned field state (device arrays of nx*ny float or double each).
+ * TM: hx, hy, dz + PML integrals icex, icey, idz.
+ * TE: hz, dx, dy + PML integrals ihz, ichx, ichy.
+ * The curl integrals are stored without the 1/dL factor of fdtd.py:85-117.
+ */
+typedef struct {
+  void* hx; void* hy; void* dz; void* icex; void* icey; void* idz;
+  void* hz; void* dx; void* dy; void* ihz; void* ichx; void* ichy;
+} cev_fdtd_state;
+
+/*
+ * One reference time step (fdtd.py:74-144) with dense sources jx, jy, jz
+ * (device arrays in the field precision, NULL = no source).  te != 0 also
+ * updates the TE fields.
+ */
+CEV_API int cev_fdtd_step(cev_fdtd_plan plan, const cev_fdtd_state* st, const void* jx, const void* jy,
+                  const void* jz, int te, cudaStream_t stream);
+
+/*
+ * E fields from the D state: ez = dz/eps_zz (TM); ex = dx/eps_xx, ey = dy/eps_yy (TE)
+ * (fdtd.py:134-142, averages of ceviche/utils.py:153-176).  NULL outputs are skipped.
+ */
+CEV_API int cev_fdtd_e_fields(cev_fdtd_plan plan, const cev_fdtd_state* st, void* ex, void* ey, void* ez,
+                      cudaStream_t stream);
+
+/* Sparse source J(t) = w_k * amps[t] at cells idx_k, and point probes. */
+typedef struct {
+  int n_src;
+  const int* src_idx;   /* device, flat cell indices */
+  const void* src_w;    /* device, field precision */
+  const void* amps;     /* device, field precision, amps[t - t_begin] */
+  int n_probe;
+  const int* probe_idx; /* device, flat cell indices */
+  void* probe_out;      /* device, field precision, [nsteps][n_probe] Ez after each step */
+} cev_fdtd_io;
+
+/*
+ * nsteps TM steps with sparse source and probes, time-blocked: each launch
+ * advances a tile by several steps in shared memory.  Bitwise the same
+ * recurrence as cev_fdtd_step.
+ */
+CEV_API int cev_fdtd_run_tm(cev_fdtd_plan plan, const cev_fdtd_state* st, int nsteps,
+                    const cev_fdtd_io* io, cudaStream_t stream);
+
+/* Workspace bytes for cev_fdtd_adjoint_tm. */
+CEV_API size_t cev_fdtd_adjoint_workspace_size(cev_fdtd_plan plan, int nsteps, int ckpt_every);
+
+/*
+ * Reverse-time adjoint of a TM run from zero fields: for the loss
+ * L = sum_t sum_p w[t][p] * Ez_t(probe_p) (w: device [nsteps][n_probe], field
+ * precision) adds dL/d(eps) to geps (device double [nx][ny]).  The forward
+ * run is checkpointed every ckpt_every steps and recomputed per segment.
+ * Replaces the autograd tape over fdtd.forward used by
+ * tests/test_gradients_fdtd.py:66-165.
+ */
+CEV_API int cev_fdtd_adjoint_tm(cev_fdtd_plan plan, int nsteps, int ckpt_every, const cev_fdtd_io* io,
+                        const void* w, double* geps, void* workspace, size_t workspace_bytes,
+                        cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CEVGPU_H_ */
