@@ -254,7 +254,7 @@ def run_ours(args):
         peak, peak_kind = _peaks()
         achieved = N * BYTES_PER_CELL_UPDATE * steps_t / (total / args.steps) / 1e9
         launches_per_run = -(-steps_t // 8)
-        cpu_v, cpu_core, cpu_wall, _ = cpu_baseline(int(os.environ.get("CEV_CPU_STEPS", "300")), 1)
+        cpu_v, cpu_core, cpu_wall, _ = cpu_baseline(int(os.environ.get("CEV_CPU_STEPS", "500")), 1)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -271,7 +271,7 @@ def run_ours(args):
                                  "across the 8 time steps of a launch"},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": "400x400 x %s FDTD steps, numpy FP64 oracle port"
-                                       % os.environ.get("CEV_CPU_STEPS", "300")},
+                                       % os.environ.get("CEV_CPU_STEPS", "500")},
             "e2e": {"value": e2e_val, "unit": UNIT,
                     "h2d_bytes_per_step": int(p["eps"].size * 8 + steps_t * 4 + 16),
                     "d2h_bytes_per_step": int(N * 4)},
