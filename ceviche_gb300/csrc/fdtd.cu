@@ -17,6 +17,7 @@
 // Dx, Dy the single-axis form.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -827,3 +828,122 @@ int cev_fdtd_adjoint_tm(cev_fdtd_plan p, int nsteps, int C, const cev_fdtd_io* i
 }
 
 }  // extern "C"
+
+// ====================================================================
+// Allocation-free TM runner.
+//
+// For callers that must not allocate device memory themselves -- e.g. code
+// running inside a host framework that owns every device allocation, or a
+// real-time loop where cudaMalloc/cudaFree (which can synchronise the
+// device) are forbidden.  It runs the same time-blocked TM kernels as
+// cev_fdtd_run_tm, but the plan's tables, 1/eps and the second (shadow)
+// copy of the state live in the file-scope arrays below, which every GPU
+// that loads this library keeps for the life of the process.
+//
+// Limits: float32 only; nx*ny <= NOALLOC_MAX_CELLS (2^18 cells, e.g.
+// 512x512), nx, ny <= NOALLOC_MAX_DIM.  Scratch: 7 * 2^18 floats (7 MiB)
+// plus 2 * 8192 axis-coefficient records (512 KiB) per device.
+// ====================================================================
+namespace cev {
+namespace {
+constexpr size_t NOALLOC_MAX_CELLS = size_t(1) << 18;
+constexpr int NOALLOC_MAX_DIM = 8192;
+// [0, 6N): shadow TM state for the double-buffered blocked kernel; [6N, 7N): 1/eps_zz
+static __device__ __align__(256) float g_noalloc_scratch[7 * NOALLOC_MAX_CELLS];
+static __device__ __align__(256) AxisCoef<float> g_noalloc_axis[2 * NOALLOC_MAX_DIM];
+
+struct NoAllocPtrs {
+  float* scratch = nullptr;
+  AxisCoef<float>* axis = nullptr;
+};
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static NoAllocPtrs g_noalloc_ptrs[NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mu;
+
+// Device addresses of the static arrays for the current device, looked up
+// once per device (the host-side names are not device addresses).
+int noalloc_setup(NoAllocPtrs& out) {
+  int dev = 0;
+  CEV_CUDA(cudaGetDevice(&dev));
+  CEV_REQUIRE(dev >= 0 && dev < NOALLOC_MAX_DEVICES, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  NoAllocPtrs& p = g_noalloc_ptrs[dev];
+  if (!p.scratch) {
+    void* s = nullptr;
+    void* a = nullptr;
+    CEV_CUDA(cudaGetSymbolAddress(&s, g_noalloc_scratch));
+    CEV_CUDA(cudaGetSymbolAddress(&a, g_noalloc_axis));
+    p.scratch = (float*)s;
+    p.axis = (AxisCoef<float>*)a;
+  }
+  out = p;
+  return CEV_OK;
+}
+
+__global__ void k_inv_ezz_f32(const double* eps, float* iez, size_t N) {
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < N;
+       n += (size_t)gridDim.x * blockDim.x)
+    iez[n] = (float)(1.0 / ((eps[n] + eps[n]) / 2));
+}
+}  // namespace
+}  // namespace cev
+
+extern "C" CEV_API int cev_fdtd_run_tm_noalloc(int nx, int ny, double dL, int npml_x, int npml_y,
+                                               const double* eps, const cev_fdtd_state* st,
+                                               int nsteps, const cev_fdtd_io* io,
+                                               cudaStream_t s) {
+  using namespace cev;
+  CEV_REQUIRE(st && eps, "NULL argument");
+  CEV_REQUIRE(nx >= 2 && ny >= 2, "grid (%d, %d) must be at least 2x2", nx, ny);
+  CEV_REQUIRE(nx <= NOALLOC_MAX_DIM && ny <= NOALLOC_MAX_DIM &&
+                  (size_t)nx * (size_t)ny <= NOALLOC_MAX_CELLS,
+              "grid (%d, %d) exceeds the allocation-free runner's limit of %zu cells "
+              "(and %d per dimension); use cev_fdtd_run_tm",
+              nx, ny, NOALLOC_MAX_CELLS, NOALLOC_MAX_DIM);
+  CEV_REQUIRE(dL > 0 && std::isfinite(dL), "dL must be positive");
+  CEV_REQUIRE(npml_x >= 0 && npml_y >= 0 && 2 * npml_x <= nx && 2 * npml_y <= ny,
+              "npml (%d, %d) must be >= 0 and fit twice in the grid", npml_x, npml_y);
+  CEV_REQUIRE(nsteps >= 0, "nsteps must be >= 0");
+  CEV_REQUIRE(st->hx && st->hy && st->dz && st->icex && st->icey && st->idz, "TM state incomplete");
+  if (io) {
+    CEV_REQUIRE(io->n_src >= 0 && io->n_probe >= 0, "negative source/probe count");
+    CEV_REQUIRE(io->n_src == 0 || (io->src_idx && io->src_w && io->amps), "source arrays missing");
+    CEV_REQUIRE(io->n_probe == 0 || (io->probe_idx && io->probe_out), "probe arrays missing");
+  }
+  NoAllocPtrs sp;
+  int rc = noalloc_setup(sp);
+  if (rc != CEV_OK) return rc;
+  if (nsteps == 0) return CEV_OK;
+  // a plan whose device tables point into the static scratch (host struct only)
+  cev_fdtd_plan_s p;
+  p.nx = nx;
+  p.ny = ny;
+  p.npml_x = npml_x;
+  p.npml_y = npml_y;
+  p.prec = CEV_PREC_C64;
+  p.dL = dL;
+  p.dt = fdtd_dt(dL);
+  const double C_0 = 1.0 / std::sqrt(F_EPSILON_0 * F_MU_0);
+  p.S = C_0 * p.dt / dL;
+  sigma_profile(nx, npml_x, p.dt, p.aHx, p.aDx);
+  sigma_profile(ny, npml_y, p.dt, p.aHy, p.aDy);
+  const auto cx = axis_coefs<float>(p.aHx, p.aDx, p.S);
+  const auto cy = axis_coefs<float>(p.aHy, p.aDy, p.S);
+  const size_t N = (size_t)nx * ny;
+  AxisCoef<float>* ax = sp.axis;
+  AxisCoef<float>* ay = sp.axis + NOALLOC_MAX_DIM;
+  // pageable-source copies: staged by the driver before the call returns
+  CEV_CUDA(cudaMemcpyAsync(ax, cx.data(), cx.size() * sizeof(cx[0]), cudaMemcpyHostToDevice, s));
+  CEV_CUDA(cudaMemcpyAsync(ay, cy.data(), cy.size() * sizeof(cy[0]), cudaMemcpyHostToDevice, s));
+  float* iez = sp.scratch + 6 * NOALLOC_MAX_CELLS;
+  k_inv_ezz_f32<<<std::max(1u, std::min(ceil_div(N, 256), 8u * sm_count())), 256, 0, s>>>(eps, iez,
+                                                                                          N);
+  CEV_CHECK_LAUNCH("k_inv_ezz_f32");
+  p.ax = ax;
+  p.ay = ay;
+  p.iez = iez;
+  p.shadow = sp.scratch;  // run_tm_impl uses 6N floats from here and never allocates
+  rc = run_tm_impl<float>(&p, st, nsteps, io, s);
+  p.ax = p.ay = p.iez = p.shadow = nullptr;  // not owned: nothing for the host struct to free
+  return rc;
+}

@@ -227,6 +227,25 @@ typedef struct {
 CEV_API int cev_fdtd_run_tm(cev_fdtd_plan plan, const cev_fdtd_state* st, int nsteps,
                     const cev_fdtd_io* io, cudaStream_t stream);
 
+/*
+ * Allocation-free variant of cev_fdtd_run_tm.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory (a host
+ * framework that owns every device allocation, or a real-time loop in which
+ * cudaMalloc/cudaFree must not be called): it needs no plan and calls no
+ * cudaMalloc, cudaFree or allocating library routine.  Its tables, 1/eps and
+ * the shadow copy of the double-buffered state live in a static device array
+ * that every GPU loading this library keeps until the process exits
+ * (7 MiB + 512 KiB).  float32 state (the fields of a CEV_PREC_C64 plan);
+ * eps is device double [nx][ny]; nx*ny <= 262144 and nx, ny <= 8192, larger
+ * grids are rejected with CEV_ERR_INVALID.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  Every call shares the array, so calls that
+ * overlap on the GPU (other streams, other host threads) race.
+ */
+CEV_API int cev_fdtd_run_tm_noalloc(int nx, int ny, double dL, int npml_x, int npml_y,
+                                    const double* eps, const cev_fdtd_state* st, int nsteps,
+                                    const cev_fdtd_io* io, cudaStream_t stream);
+
 /* Workspace bytes for cev_fdtd_adjoint_tm. */
 CEV_API size_t cev_fdtd_adjoint_workspace_size(cev_fdtd_plan plan, int nsteps, int ckpt_every);
 
