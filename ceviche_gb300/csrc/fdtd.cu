@@ -17,6 +17,7 @@
 // Dx, Dy the single-axis form.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <mutex>
 #include <vector>
 
@@ -259,11 +260,15 @@ __global__ void k_probe(const R* dz, const R* iez, int np, const int* idx, R* ou
 }
 
 // ------------------------------------------------------- time-blocked TM
-// One CTA advances a TI x TJ tile by K steps in shared memory, computing a
-// halo of K cells that shrinks by one per step (H needs Ez at i+1, j+1; D
-// needs H at i-1, j-1).  State is double-buffered in global memory.
-constexpr int TB_TI = 32, TB_TJ = 32, TB_KMAX = 8, TB_THREADS = 256;
-
+// One CTA advances a TI x TJ tile by up to K steps.  It loads the tile plus a
+// halo of K cells; each cell's state (Hx, Hy, Dz, 1/eps, PML integrals,
+// source weight) stays in registers of its owning thread for the whole
+// launch, and only Ez (after the D phase) and Hx, Hy (after the H phase) go
+// through shared memory.  The halo's valid zone shrinks by one cell per step
+// (H needs Ez at i+1, j+1; D needs H at i-1, j-1), so after K steps the
+// interior is exact.  At the region's edge the missing neighbour is replaced
+// by the cell itself: those cells are outside the valid zone and never reach
+// the interior.  The state is double-buffered in global memory.
 template <typename R>
 struct TBArgs {
   int nx, ny, K, t0;
@@ -282,248 +287,303 @@ struct TBArgs {
   R* probe_out;   // [t][np]
 };
 
-template <typename R>
-__global__ void __launch_bounds__(TB_THREADS) k_tm_blocked(TBArgs<R> a) {
+template <typename R, int TI, int TJ, int K, int NT>
+struct Tile {
+  static constexpr int RI = TI + 2 * K, RJ = TJ + 2 * K, RN = RI * RJ;
+  static constexpr int CPT = (RN + NT - 1) / NT;
+  // sEz, sHx, sHy, sW (source weights), sIx, sIy, sId (PML integrals) [RN];
+  // per-row x tables (5 x RI) and per-column y tables (5 x RJ); amps [K]
+  static constexpr size_t smem =
+      7 * (size_t)RN * sizeof(R) + 5 * (size_t)(RI + RJ) * sizeof(R) + (size_t)K * sizeof(R);
+};
+
+template <typename R, int TI, int TJ, int K, int NT>
+__global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
+  using T = Tile<R, TI, TJ, K, NT>;
+  constexpr int RI = T::RI, RJ = T::RJ, RN = T::RN, CPT = T::CPT;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const int K = a.K;
-  const int RI = TB_TI + 2 * K, RJ = TB_TJ + 2 * K;
-  const int RN = RI * RJ;
-  R* sHx = (R*)smraw;
+  R* sEz = (R*)smraw;
+  R* sHx = sEz + RN;
   R* sHy = sHx + RN;
-  R* sDz = sHy + RN;
-  R* sIe = sDz + RN;
-  R* sCx = sIe + RN;  // ICEx'
-  R* sCy = sCx + RN;  // ICEy'
-  R* sId = sCy + RN;  // IDz
-  AxisCoef<R>* cX = (AxisCoef<R>*)(sId + RN);
-  AxisCoef<R>* cY = cX + RI;
-  const int gi0 = blockIdx.y * TB_TI - K;  // region origin (may be negative)
-  const int gj0 = blockIdx.x * TB_TJ - K;
+  R* sW = sHy + RN;   // source weight per region cell
+  R* sIx = sW + RN;   // ICEx' (PML tiles only)
+  R* sIy = sIx + RN;  // ICEy'
+  R* sId = sIy + RN;  // IDz
+  // structure-of-arrays coefficient tables (conflict-free column access)
+  R* xf1 = sId + RN;  // f1H along x (rows)
+  R* xf2 = xf1 + RI;  // f2H
+  R* xg3 = xf2 + RI;  // 2 aH
+  R* xaD = xg3 + RI;  // aD
+  R* xpD = xaD + RI;  // pD
+  R* yf1 = xpD + RI;
+  R* yf2 = yf1 + RJ;
+  R* yg3 = yf2 + RJ;
+  R* yaD = yg3 + RJ;
+  R* ypD = yaD + RJ;
+  R* sAmp = ypD + RJ;
+  const int nst = a.K;  // steps of this launch, <= K
+  const int gi0 = blockIdx.y * TI - K, gj0 = blockIdx.x * TJ - K;
   const int tid = threadIdx.x;
-  auto gi = [&](int r) { int v = gi0 + r; v %= a.nx; return v < 0 ? v + a.nx : v; };
-  auto gj = [&](int c) { int v = gj0 + c; v %= a.ny; return v < 0 ? v + a.ny : v; };
-  for (int r = tid; r < RI; r += TB_THREADS) cX[r] = a.ax[gi(r)];
-  for (int c = tid; c < RJ; c += TB_THREADS) cY[c] = a.ay[gj(c)];
-  __syncthreads();
-  int pml_local = 0;
-  for (int r = tid; r < RI; r += TB_THREADS) pml_local |= (cX[r].aH != R(0)) | (cX[r].aD != R(0));
-  for (int c = tid; c < RJ; c += TB_THREADS) pml_local |= (cY[c].aH != R(0)) | (cY[c].aD != R(0));
-  const bool pml = __syncthreads_or(pml_local);
-  for (int q = tid; q < RN; q += TB_THREADS) {
-    const int r = q / RJ, c = q - r * RJ;
-    const size_t n = (size_t)gi(r) * a.ny + gj(c);
-    sHx[q] = a.hx_i[n];
-    sHy[q] = a.hy_i[n];
-    sDz[q] = a.dz_i[n];
-    sIe[q] = a.iez[n];
-    if (pml) {
-      sCx[q] = a.icex_i[n];
-      sCy[q] = a.icey_i[n];
-      sId[q] = a.idz_i[n];
-    }
+  auto gi = [&](int r) { int v = (gi0 + r) % a.nx; return v < 0 ? v + a.nx : v; };
+  auto gj = [&](int c) { int v = (gj0 + c) % a.ny; return v < 0 ? v + a.ny : v; };
+  int pl = 0;
+  for (int r = tid; r < RI; r += NT) {
+    const AxisCoef<R> c = a.ax[gi(r)];
+    xf1[r] = c.f1H; xf2[r] = c.f2H; xg3[r] = R(2) * c.aH; xaD[r] = c.aD; xpD[r] = c.pD;
+    pl |= (c.aH != R(0)) | (c.aD != R(0));
+  }
+  for (int q = tid; q < RJ; q += NT) {
+    const AxisCoef<R> c = a.ay[gj(q)];
+    yf1[q] = c.f1H; yf2[q] = c.f2H; yg3[q] = R(2) * c.aH; yaD[q] = c.aD; ypD[q] = c.pD;
+    pl |= (c.aH != R(0)) | (c.aD != R(0));
+  }
+  for (int st = tid; st < nst; st += NT) sAmp[st] = a.ns > 0 ? a.amps[a.t0 + st] : R(0);
+  for (int q = tid; q < RN; q += NT) sW[q] = R(0);
+  const bool pml = __syncthreads_or(pl);
+  for (int k = tid; k < a.ns; k += NT) {
+    const int n = a.src_idx[k];
+    const int ii = n / a.ny, jj = n - ii * a.ny;
+    int r = (ii - gi0) % a.nx;
+    if (r < 0) r += a.nx;
+    int c = (jj - gj0) % a.ny;
+    if (c < 0) c += a.ny;
+    if (r < RI && c < RJ) atomicAdd(&sW[r * RJ + c], a.src_w[k]);
   }
   __syncthreads();
-  for (int s = 0; s < K; ++s) {
-    // H phase on [0, RI-1) x [0, RJ-1)
-    for (int q = tid; q < RN; q += TB_THREADS) {
+  R hx[CPT], hy[CPT], dz[CPT], ie[CPT];
+  unsigned srcmask = 0;  // bit k: owned cell k has a source
+  unsigned pmlmask = 0;  // bit k: some cell of this warp's slot k lies on a PML row/column
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int q = tid + k * NT;
+    hx[k] = hy[k] = dz[k] = ie[k] = R(0);
+    bool cell_pml = false;
+    if (q < RN) {
       const int r = q / RJ, c = q - r * RJ;
-      if (r >= RI - 1 || c >= RJ - 1) continue;
-      const R ez = sDz[q] * sIe[q];
-      const R dEy = sDz[q + 1] * sIe[q + 1] - ez;
-      const R dEx = -(sDz[q + RJ] * sIe[q + RJ] - ez);
-      const AxisCoef<R> cx = cX[r], cy = cY[c];
-      R icx = R(0), icy = R(0);
+      const size_t n = (size_t)gi(r) * a.ny + gj(c);
+      hx[k] = a.hx_i[n];
+      hy[k] = a.hy_i[n];
+      dz[k] = a.dz_i[n];
+      ie[k] = a.iez[n];
+      cell_pml = (xg3[r] != R(0)) | (yg3[c] != R(0)) | (xaD[r] != R(0)) | (yaD[c] != R(0));
       if (pml) {
-        if (cx.aH != R(0)) { icx = sCx[q] + dEy; sCx[q] = icx; }
-        if (cy.aH != R(0)) { icy = sCy[q] + dEx; sCy[q] = icy; }
+        sIx[q] = a.icex_i[n];
+        sIy[q] = a.icey_i[n];
+        sId[q] = a.idz_i[n];
       }
-      sHx[q] = cy.f1H * sHx[q] - cy.f2H * (dEy + R(2) * cx.aH * icx);
-      sHy[q] = cx.f1H * sHy[q] - cx.f2H * (dEx + R(2) * cy.aH * icy);
+      if (sW[q] != R(0)) srcmask |= 1u << k;
+      sEz[q] = dz[k] * ie[k];
     }
-    __syncthreads();
-    // D phase on [1, RI) x [1, RJ)
-    for (int q = tid; q < RN; q += TB_THREADS) {
-      const int r = q / RJ, c = q - r * RJ;
-      if (r < 1 || c < 1) continue;
-      const R ch = (sHy[q] - sHy[q - RJ]) - (sHx[q] - sHx[q - 1]);
-      R m1, m2, m4;
-      dz_coefs(cX[r], cY[c], a.S, m1, m2, m4);
-      const R dz = sDz[q];
-      R id = R(0);
-      if (pml && m4 != R(0)) { id = sId[q] + dz; sId[q] = id; }
-      sDz[q] = m1 * dz + m2 * ch + m4 * id;
-    }
-    __syncthreads();
-    const int t = a.t0 + s;
-    if (a.ns > 0) {
-      const R amp = a.amps[t];
-      for (int k = tid; k < a.ns; k += TB_THREADS) {
-        const int n = a.src_idx[k];
-        const int ii = n / a.ny, jj = n - ii * a.ny;
-        int r = (ii - gi0) % a.nx; if (r < 0) r += a.nx;
-        int c = (jj - gj0) % a.ny; if (c < 0) c += a.ny;
-        if (r < RI && c < RJ) sDz[r * RJ + c] += a.src_w[k] * amp;
+    if (__any_sync(0xffffffffu, cell_pml)) pmlmask |= 1u << k;
+  }
+  __syncthreads();
+  const R S = a.S;
+  for (int st = 0; st < nst; ++st) {
+    const R amp = sAmp[st];
+    if (!pml) {
+      // no PML cell in the region: a = 0, so f1 = 1, f2 = S, mDz1 = 1,
+      // mDz2 = S, mDz4 = 0 and no integral is accumulated
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int q = tid + k * NT;
+        if (q < RN) {
+          const int r = q / RJ, c = q - r * RJ;
+          const R ez = sEz[q];
+          const R ezr = (c < RJ - 1) ? sEz[q + 1] : ez;
+          const R ezd = (r < RI - 1) ? sEz[q + RJ] : ez;
+          hx[k] = hx[k] - S * (ezr - ez);
+          hy[k] = hy[k] - S * (-(ezd - ez));
+          sHx[q] = hx[k];
+          sHy[q] = hy[k];
+        }
       }
       __syncthreads();
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int q = tid + k * NT;
+        if (q < RN) {
+          const int r = q / RJ, c = q - r * RJ;
+          const R hyu = (r > 0) ? sHy[q - RJ] : hy[k];
+          const R hxl = (c > 0) ? sHx[q - 1] : hx[k];
+          R v = dz[k] + S * ((hy[k] - hyu) - (hx[k] - hxl));
+          if (srcmask & (1u << k)) v += sW[q] * amp;
+          dz[k] = v;
+          sEz[q] = v * ie[k];
+        }
+      }
+    } else {
+      // PML tile: warp slots without a PML cell still take the a = 0 form
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int q = tid + k * NT;
+        if (q < RN) {
+          const int r = q / RJ, c = q - r * RJ;
+          const R ez = sEz[q];
+          const R ezr = (c < RJ - 1) ? sEz[q + 1] : ez;
+          const R ezd = (r < RI - 1) ? sEz[q + RJ] : ez;
+          const R dEy = ezr - ez;
+          const R dEx = -(ezd - ez);
+          if (!(pmlmask & (1u << k))) {
+            hx[k] = hx[k] - S * dEy;
+            hy[k] = hy[k] - S * dEx;
+          } else {
+            const R gx = xg3[r], gy = yg3[c];
+            R ix = R(0), iy = R(0);
+            if (gx != R(0)) { ix = sIx[q] + dEy; sIx[q] = ix; }
+            if (gy != R(0)) { iy = sIy[q] + dEx; sIy[q] = iy; }
+            hx[k] = yf1[c] * hx[k] - yf2[c] * (dEy + gx * ix);
+            hy[k] = xf1[r] * hy[k] - xf2[r] * (dEx + gy * iy);
+          }
+          sHx[q] = hx[k];
+          sHy[q] = hy[k];
+        }
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int q = tid + k * NT;
+        if (q < RN) {
+          const int r = q / RJ, c = q - r * RJ;
+          const R hyu = (r > 0) ? sHy[q - RJ] : hy[k];
+          const R hxl = (c > 0) ? sHx[q - 1] : hx[k];
+          const R ch = (hy[k] - hyu) - (hx[k] - hxl);
+          R v;
+          if (!(pmlmask & (1u << k))) {
+            v = dz[k] + S * ch;
+          } else {
+            const R ax = xaD[r], ay = yaD[c];
+            const R pd = xpD[r] * ypD[c];
+            const R m1 = (R(1) - ax - ay - ax * ay) * pd;
+            const R m2 = S * pd;
+            const R m4 = R(-4) * ax * ay * pd;
+            R id = R(0);
+            if (m4 != R(0)) { id = sId[q] + dz[k]; sId[q] = id; }
+            v = m1 * dz[k] + m2 * ch + m4 * id;
+          }
+          if (srcmask & (1u << k)) v += sW[q] * amp;
+          dz[k] = v;
+          sEz[q] = v * ie[k];
+        }
+      }
     }
-    for (int k = tid; k < a.np; k += TB_THREADS) {
+    __syncthreads();
+    // probes of interior cells: Ez after this step
+    for (int k = tid; k < a.np; k += NT) {
       const int n = a.probe_idx[k];
       const int ii = n / a.ny, jj = n - ii * a.ny;
       const int r = ii - gi0, c = jj - gj0;
-      if (r >= K && r < K + TB_TI && c >= K && c < K + TB_TJ) {
-        const int q = r * RJ + c;
-        a.probe_out[(size_t)t * a.np + k] = sDz[q] * sIe[q];
-      }
+      if (r >= K && r < K + TI && c >= K && c < K + TJ)
+        a.probe_out[(size_t)(a.t0 + st) * a.np + k] = sEz[r * RJ + c];
     }
   }
   // write back the tile interior
-  for (int q = tid; q < TB_TI * TB_TJ; q += TB_THREADS) {
-    const int r = q / TB_TJ + K, c = q % TB_TJ + K;
-    const int ii = gi0 + r, jj = gj0 + c;
-    if (ii >= a.nx || jj >= a.ny) continue;
-    const size_t n = (size_t)ii * a.ny + jj;
-    const int p = r * RJ + c;
-    a.hx_o[n] = sHx[p];
-    a.hy_o[n] = sHy[p];
-    a.dz_o[n] = sDz[p];
-    if (pml) {
-      a.icex_o[n] = sCx[p];
-      a.icey_o[n] = sCy[p];
-      a.idz_o[n] = sId[p];
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int q = tid + k * NT;
+    if (q < RN) {
+      const int r = q / RJ, c = q - r * RJ;
+      const int ii = gi0 + r, jj = gj0 + c;
+      if (r >= K && r < K + TI && c >= K && c < K + TJ && ii < a.nx && jj < a.ny) {
+        const size_t n = (size_t)ii * a.ny + jj;
+        a.hx_o[n] = hx[k];
+        a.hy_o[n] = hy[k];
+        a.dz_o[n] = dz[k];
+        if (pml) {
+          a.icex_o[n] = sIx[q];
+          a.icey_o[n] = sIy[q];
+          a.idz_o[n] = sId[q];
+        }
+      }
     }
   }
 }
 
-template <typename R>
-static size_t tb_smem(int K) {
-  const int RI = TB_TI + 2 * K, RJ = TB_TJ + 2 * K;
-  return (size_t)7 * RI * RJ * sizeof(R) + (size_t)(RI + RJ) * sizeof(AxisCoef<R>);
-}
+// Tile configurations (TI, TJ, K, threads); the launcher picks one per grid.
+struct TileCfg {
+  int ti, tj, k, nt;
+};
+constexpr TileCfg TILE_CFGS[] = {{48, 48, 8, 1024}, {48, 48, 8, 512}, {32, 48, 8, 512},
+                                 {26, 48, 8, 512},  {25, 50, 8, 512}, {16, 48, 8, 512}};
+constexpr int N_TILE_CFGS = sizeof(TILE_CFGS) / sizeof(TILE_CFGS[0]);
 
-// ------------------------------------------------------------ TM adjoint
-// Reverse of one TM step n (see header comment for the forward form):
-//   aCH = m2 aDz ; aIDz += m4 aDz ; aDz_prev = m1 aDz + aIDz
-//   aHy_t = aHy + aCH - aCH[i+1,j] ; aHx_t = aHx - (aCH - aCH[i,j+1])
-//   aHx = f1Hy aHx_t ; t = -f2Hy aHx_t ; aICEx += 2aHx t ; adEy = t + aICEx  (same for y)
-//   aEz^{n-1} = w_{n-1} p + adEy[i,j-1] - adEy + adEx - adEx[i-1,j]
-//   aDz^{n-1} = aDz_prev + aEz^{n-1}/eps ; geps += aEz^{n-1} (-Dz^{n-1}/eps^2)
-template <typename R>
-struct AdjArgs {
-  int nx, ny;
-  R* ahx; R* ahy; R* adz; R* aicex; R* aicey; R* aidz;
-  R* ach; R* adey; R* adex; R* adzp;
-  const R* iez;
-  const AxisCoef<R>* ax;
-  const AxisCoef<R>* ay;
-  R S;
+template <typename R, int I>
+struct TileLauncher {
+  static constexpr TileCfg c = TILE_CFGS[I];
+  using T = Tile<R, c.ti, c.tj, c.k, c.nt>;
+  static int prepare() {
+    CEV_CUDA(cudaFuncSetAttribute(k_tm_tile<R, c.ti, c.tj, c.k, c.nt>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem));
+    return CEV_OK;
+  }
+  static void launch(dim3 g, const TBArgs<R>& a, cudaStream_t s) {
+    k_tm_tile<R, c.ti, c.tj, c.k, c.nt><<<g, c.nt, T::smem, s>>>(a);
+  }
+  static constexpr size_t smem_bytes = T::smem;
+  static int per_sm() {
+    int n = 0;
+    if (prepare() != CEV_OK) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tm_tile<R, c.ti, c.tj, c.k, c.nt>,
+                                                      c.nt, T::smem) != cudaSuccess || n < 1)
+      n = 1;
+    return n;
+  }
 };
 
-template <typename R>
-__global__ void k_adj_a(AdjArgs<R> a) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= a.nx || j >= a.ny) return;
-  const size_t n = (size_t)i * a.ny + j;
-  R m1, m2, m4;
-  dz_coefs(a.ax[i], a.ay[j], a.S, m1, m2, m4);
-  const R adz = a.adz[n];
-  a.ach[n] = m2 * adz;
-  R aid = a.aidz[n];
-  if (m4 != R(0)) { aid += m4 * adz; a.aidz[n] = aid; }
-  a.adzp[n] = m1 * adz + aid;
-}
-
-template <typename R>
-__global__ void k_adj_b(AdjArgs<R> a) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= a.nx || j >= a.ny) return;
-  const size_t n = (size_t)i * a.ny + j;
-  const int ip = i + 1 == a.nx ? 0 : i + 1, jp = j + 1 == a.ny ? 0 : j + 1;
-  const R ach = a.ach[n];
-  const R ahy_t = a.ahy[n] + ach - a.ach[(size_t)ip * a.ny + j];
-  const R ahx_t = a.ahx[n] - (ach - a.ach[(size_t)i * a.ny + jp]);
-  const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
-  a.ahx[n] = cy.f1H * ahx_t;
-  R t = -cy.f2H * ahx_t;
-  R ai = R(0);
-  if (cx.aH != R(0)) { ai = a.aicex[n] + R(2) * cx.aH * t; a.aicex[n] = ai; }
-  a.adey[n] = t + ai;
-  a.ahy[n] = cx.f1H * ahy_t;
-  t = -cx.f2H * ahy_t;
-  ai = R(0);
-  if (cy.aH != R(0)) { ai = a.aicey[n] + R(2) * cy.aH * t; a.aicey[n] = ai; }
-  a.adex[n] = t + ai;
-}
-
-// finishes the step: aDz for Ez^{n-1}; gradient term with Dz^{n-1}
-template <typename R>
-__global__ void k_adj_c(AdjArgs<R> a, const R* dz_prev, double* geps, int np, const int* pidx,
-                        const R* wrow) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= a.nx || j >= a.ny) return;
-  const size_t n = (size_t)i * a.ny + j;
-  const int im = i == 0 ? a.nx - 1 : i - 1, jm = j == 0 ? a.ny - 1 : j - 1;
-  R aez = a.adey[(size_t)i * a.ny + jm] - a.adey[n] + a.adex[n] - a.adex[(size_t)im * a.ny + j];
-  if (wrow) {
-    for (int k = 0; k < np; ++k)
-      if (pidx[k] == (int)n) aez += wrow[k];
+template <typename R, int I = 0>
+size_t tile_smem(int cfg) {
+  if constexpr (I < N_TILE_CFGS) {
+    if (cfg == I) return TileLauncher<R, I>::smem_bytes;
+    return tile_smem<R, I + 1>(cfg);
+  } else {
+    return 0;
   }
-  const R ie = a.iez[n];
-  a.adz[n] = a.adzp[n] + aez * ie;
-  if (dz_prev) geps[n] += (double)aez * (double)(-dz_prev[n] * ie * ie);
 }
 
-// initial adjoint for the last output step T: aEz^T = w_T p
-template <typename R>
-__global__ void k_adj_init(int N, R* adz, const R* iez, double* geps, const R* dz_T, int np,
-                           const int* pidx, const R* wrow) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= np) return;
-  const int n = pidx[k];
-  const R ie = iez[n];
-  atomicAdd(&adz[n], wrow[k] * ie);
-  atomicAdd(&geps[n], (double)wrow[k] * (double)(-dz_T[n] * ie * ie));
-}
-
-dim3 grid2(int nx, int ny, dim3 blk) { return dim3((ny + blk.x - 1) / blk.x, (nx + blk.y - 1) / blk.y, 1); }
-
-template <typename R>
-TMArgs<R> tm_args(cev_fdtd_plan p, const cev_fdtd_state* st, const R* jz) {
-  TMArgs<R> a;
-  a.nx = p->nx;
-  a.ny = p->ny;
-  a.hx = (R*)st->hx; a.hy = (R*)st->hy; a.dz = (R*)st->dz;
-  a.icex = (R*)st->icex; a.icey = (R*)st->icey; a.idz = (R*)st->idz;
-  a.iez = (const R*)p->iez;
-  a.ax = (const AxisCoef<R>*)p->ax;
-  a.ay = (const AxisCoef<R>*)p->ay;
-  a.S = (R)p->S;
-  a.jz = jz;
-  return a;
-}
-
-template <typename R>
-int step_impl(cev_fdtd_plan p, const cev_fdtd_state* st, const R* jx, const R* jy, const R* jz,
-              int te, cudaStream_t s) {
-  const dim3 blk(32, 8);
-  const dim3 g = grid2(p->nx, p->ny, blk);
-  TMArgs<R> a = tm_args<R>(p, st, jz);
-  k_tm_h<R><<<g, blk, 0, s>>>(a);
-  if (te) {
-    TEArgs<R> e;
-    e.nx = p->nx; e.ny = p->ny;
-    e.hz = (R*)st->hz; e.dx = (R*)st->dx; e.dy = (R*)st->dy;
-    e.ihz = (R*)st->ihz; e.ichx = (R*)st->ichx; e.ichy = (R*)st->ichy;
-    e.iexx = (const R*)p->iexx; e.ieyy = (const R*)p->ieyy;
-    e.ax = a.ax; e.ay = a.ay; e.S = a.S; e.jx = jx; e.jy = jy;
-    k_te_h<R><<<g, blk, 0, s>>>(e);
-    k_te_d<R><<<g, blk, 0, s>>>(e);
+template <typename R, int I = 0>
+int tile_per_sm(int cfg) {
+  if constexpr (I < N_TILE_CFGS) {
+    if (cfg == I) return TileLauncher<R, I>::per_sm();
+    return tile_per_sm<R, I + 1>(cfg);
+  } else {
+    return 1;
   }
-  k_tm_d<R><<<g, blk, 0, s>>>(a);
-  CEV_CHECK_LAUNCH("fdtd step");
-  return CEV_OK;
+}
+
+template <typename R, int I = 0>
+int tile_dispatch(int cfg, bool prepare, dim3 g, const TBArgs<R>& a, cudaStream_t s) {
+  if constexpr (I < N_TILE_CFGS) {
+    if (cfg == I) {
+      if (prepare) return TileLauncher<R, I>::prepare();
+      TileLauncher<R, I>::launch(g, a, s);
+      return CEV_OK;
+    }
+    return tile_dispatch<R, I + 1>(cfg, prepare, g, a, s);
+  } else {
+    set_error("bad tile configuration %d", cfg);
+    return CEV_ERR_INVALID;
+  }
+}
+
+// Tile choice: CEV_FDTD_TILE=<index> overrides.  Otherwise 48x48 tiles with
+// 1024 threads (measured best from 1024^2 to 4096^2), or 32x48 tiles with 512
+// threads when 48x48 tiles would not fill the GPU once (measured best at 400^2).
+template <typename R>
+static int pick_tile(int nx, int ny) {
+  auto fits = [&](int v) {
+    const TileCfg c = TILE_CFGS[v];
+    return nx >= c.ti + 2 * c.k && ny >= c.tj + 2 * c.k && tile_smem<R>(v) <= 227 * 1024;
+  };
+  if (const char* e = std::getenv("CEV_FDTD_TILE")) {
+    const int v = std::atoi(e);
+    if (v >= 0 && v < N_TILE_CFGS && fits(v)) return v;
+  }
+  const long tiles0 = (long)((nx + 47) / 48) * ((ny + 47) / 48);
+  const int order_big[] = {0, 1, 2, 5};
+  const int order_small[] = {2, 3, 5, 0};
+  const int* order = tiles0 >= sm_count() ? order_big : order_small;
+  for (int k = 0; k < 4; ++k)
+    if (fits(order[k])) return order[k];
+  return -1;
 }
 
 template <typename R>
@@ -531,9 +591,9 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
                 cudaStream_t s) {
   const size_t N = p->n();
   const int ns = io ? io->n_src : 0, np = io ? io->n_probe : 0;
-  const bool blocked = p->nx >= TB_TI + 2 * TB_KMAX && p->ny >= TB_TJ + 2 * TB_KMAX;
-  if (!blocked) {
-    // small grids: per-step kernels
+  const int cfg = pick_tile<R>(p->nx, p->ny);
+  if (cfg < 0) {
+    // grids smaller than one tile region: per-step kernels
     for (int t = 0; t < nsteps; ++t) {
       int rc = step_impl<R>(p, st, nullptr, nullptr, nullptr, 0, s);
       if (rc != CEV_OK) return rc;
@@ -555,21 +615,21 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
   CEV_CUDA(cudaMemcpyAsync(bufB[3], bufA[3], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   CEV_CUDA(cudaMemcpyAsync(bufB[4], bufA[4], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   CEV_CUDA(cudaMemcpyAsync(bufB[5], bufA[5], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
-  const int K = TB_KMAX;
-  const size_t smem = tb_smem<R>(K);
-  static bool attr_set[2] = {false, false};
-  if (!attr_set[sizeof(R) == 8]) {
-    CEV_CUDA(cudaFuncSetAttribute(k_tm_blocked<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)tb_smem<R>(TB_KMAX)));
-    attr_set[sizeof(R) == 8] = true;
+  static bool prepared[2][N_TILE_CFGS] = {};
+  TBArgs<R> a{};
+  if (!prepared[sizeof(R) == 8][cfg]) {
+    int rc = tile_dispatch<R>(cfg, true, dim3(), a, s);
+    if (rc != CEV_OK) return rc;
+    prepared[sizeof(R) == 8][cfg] = true;
   }
-  const dim3 g((p->ny + TB_TJ - 1) / TB_TJ, (p->nx + TB_TI - 1) / TB_TI, 1);
+  const TileCfg tc = TILE_CFGS[cfg];
+  const int K = tc.k;
+  const dim3 g((p->ny + tc.tj - 1) / tc.tj, (p->nx + tc.ti - 1) / tc.ti, 1);
   R** in = bufA;
   R** out = bufB;
   int t = 0;
   while (t < nsteps) {
     const int k = std::min(K, nsteps - t);
-    TBArgs<R> a;
     a.nx = p->nx; a.ny = p->ny; a.K = k; a.t0 = t;
     a.hx_i = in[0]; a.hy_i = in[1]; a.dz_i = in[2]; a.icex_i = in[3]; a.icey_i = in[4]; a.idz_i = in[5];
     a.hx_o = out[0]; a.hy_o = out[1]; a.dz_o = out[2]; a.icex_o = out[3]; a.icey_o = out[4]; a.idz_o = out[5];
@@ -584,8 +644,8 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
     a.np = np;
     a.probe_idx = np ? io->probe_idx : nullptr;
     a.probe_out = np ? (R*)io->probe_out : nullptr;
-    k_tm_blocked<R><<<g, TB_THREADS, smem, s>>>(a);
-    CEV_CHECK_LAUNCH("k_tm_blocked");
+    tile_dispatch<R>(cfg, false, g, a, s);
+    CEV_CHECK_LAUNCH("k_tm_tile");
     std::swap(in, out);
     t += k;
   }
