@@ -48,6 +48,13 @@ def build(verbose=False, force=False, extra=()):
     objs = [os.path.join(OBJDIR, os.path.basename(s)[:-3] + ".o") for s in sources]
 
     def run(cmd):
+        if "-c" in cmd:
+            # never leave a stale object behind a failed compile
+            obj = cmd[cmd.index("-o") + 1]
+            if os.path.exists(obj):
+                os.remove(obj)
+            if os.path.exists(LIB):
+                os.remove(LIB)
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

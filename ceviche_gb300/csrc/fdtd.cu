@@ -586,6 +586,132 @@ static int pick_tile(int nx, int ny) {
   return -1;
 }
 
+// ------------------------------------------------------------ TM adjoint
+// Reverse of one TM step n (see header comment for the forward form):
+//   aCH = m2 aDz ; aIDz += m4 aDz ; aDz_prev = m1 aDz + aIDz
+//   aHy_t = aHy + aCH - aCH[i+1,j] ; aHx_t = aHx - (aCH - aCH[i,j+1])
+//   aHx = f1Hy aHx_t ; t = -f2Hy aHx_t ; aICEx += 2aHx t ; adEy = t + aICEx  (same for y)
+//   aEz^{n-1} = w_{n-1} p + adEy[i,j-1] - adEy + adEx - adEx[i-1,j]
+//   aDz^{n-1} = aDz_prev + aEz^{n-1}/eps ; geps += aEz^{n-1} (-Dz^{n-1}/eps^2)
+template <typename R>
+struct AdjArgs {
+  int nx, ny;
+  R* ahx; R* ahy; R* adz; R* aicex; R* aicey; R* aidz;
+  R* ach; R* adey; R* adex; R* adzp;
+  const R* iez;
+  const AxisCoef<R>* ax;
+  const AxisCoef<R>* ay;
+  R S;
+};
+
+template <typename R>
+__global__ void k_adj_a(AdjArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  R m1, m2, m4;
+  dz_coefs(a.ax[i], a.ay[j], a.S, m1, m2, m4);
+  const R adz = a.adz[n];
+  a.ach[n] = m2 * adz;
+  R aid = a.aidz[n];
+  if (m4 != R(0)) { aid += m4 * adz; a.aidz[n] = aid; }
+  a.adzp[n] = m1 * adz + aid;
+}
+
+template <typename R>
+__global__ void k_adj_b(AdjArgs<R> a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int ip = i + 1 == a.nx ? 0 : i + 1, jp = j + 1 == a.ny ? 0 : j + 1;
+  const R ach = a.ach[n];
+  const R ahy_t = a.ahy[n] + ach - a.ach[(size_t)ip * a.ny + j];
+  const R ahx_t = a.ahx[n] - (ach - a.ach[(size_t)i * a.ny + jp]);
+  const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
+  a.ahx[n] = cy.f1H * ahx_t;
+  R t = -cy.f2H * ahx_t;
+  R ai = R(0);
+  if (cx.aH != R(0)) { ai = a.aicex[n] + R(2) * cx.aH * t; a.aicex[n] = ai; }
+  a.adey[n] = t + ai;
+  a.ahy[n] = cx.f1H * ahy_t;
+  t = -cx.f2H * ahy_t;
+  ai = R(0);
+  if (cy.aH != R(0)) { ai = a.aicey[n] + R(2) * cy.aH * t; a.aicey[n] = ai; }
+  a.adex[n] = t + ai;
+}
+
+// finishes the step: aDz for Ez^{n-1}; gradient term with Dz^{n-1}
+template <typename R>
+__global__ void k_adj_c(AdjArgs<R> a, const R* dz_prev, double* geps, int np, const int* pidx,
+                        const R* wrow) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const int im = i == 0 ? a.nx - 1 : i - 1, jm = j == 0 ? a.ny - 1 : j - 1;
+  R aez = a.adey[(size_t)i * a.ny + jm] - a.adey[n] + a.adex[n] - a.adex[(size_t)im * a.ny + j];
+  if (wrow) {
+    for (int k = 0; k < np; ++k)
+      if (pidx[k] == (int)n) aez += wrow[k];
+  }
+  const R ie = a.iez[n];
+  a.adz[n] = a.adzp[n] + aez * ie;
+  if (dz_prev) geps[n] += (double)aez * (double)(-dz_prev[n] * ie * ie);
+}
+
+// initial adjoint for the last output step T: aEz^T = w_T p
+template <typename R>
+__global__ void k_adj_init(int N, R* adz, const R* iez, double* geps, const R* dz_T, int np,
+                           const int* pidx, const R* wrow) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  const int n = pidx[k];
+  const R ie = iez[n];
+  atomicAdd(&adz[n], wrow[k] * ie);
+  atomicAdd(&geps[n], (double)wrow[k] * (double)(-dz_T[n] * ie * ie));
+}
+
+dim3 grid2(int nx, int ny, dim3 blk) { return dim3((ny + blk.x - 1) / blk.x, (nx + blk.y - 1) / blk.y, 1); }
+
+template <typename R>
+TMArgs<R> tm_args(cev_fdtd_plan p, const cev_fdtd_state* st, const R* jz) {
+  TMArgs<R> a;
+  a.nx = p->nx;
+  a.ny = p->ny;
+  a.hx = (R*)st->hx; a.hy = (R*)st->hy; a.dz = (R*)st->dz;
+  a.icex = (R*)st->icex; a.icey = (R*)st->icey; a.idz = (R*)st->idz;
+  a.iez = (const R*)p->iez;
+  a.ax = (const AxisCoef<R>*)p->ax;
+  a.ay = (const AxisCoef<R>*)p->ay;
+  a.S = (R)p->S;
+  a.jz = jz;
+  return a;
+}
+
+template <typename R>
+int step_impl(cev_fdtd_plan p, const cev_fdtd_state* st, const R* jx, const R* jy, const R* jz,
+              int te, cudaStream_t s) {
+  const dim3 blk(32, 8);
+  const dim3 g = grid2(p->nx, p->ny, blk);
+  TMArgs<R> a = tm_args<R>(p, st, jz);
+  k_tm_h<R><<<g, blk, 0, s>>>(a);
+  if (te) {
+    TEArgs<R> e;
+    e.nx = p->nx; e.ny = p->ny;
+    e.hz = (R*)st->hz; e.dx = (R*)st->dx; e.dy = (R*)st->dy;
+    e.ihz = (R*)st->ihz; e.ichx = (R*)st->ichx; e.ichy = (R*)st->ichy;
+    e.iexx = (const R*)p->iexx; e.ieyy = (const R*)p->ieyy;
+    e.ax = a.ax; e.ay = a.ay; e.S = a.S; e.jx = jx; e.jy = jy;
+    k_te_h<R><<<g, blk, 0, s>>>(e);
+    k_te_d<R><<<g, blk, 0, s>>>(e);
+  }
+  k_tm_d<R><<<g, blk, 0, s>>>(a);
+  CEV_CHECK_LAUNCH("fdtd step");
+  return CEV_OK;
+}
+
 template <typename R>
 int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev_fdtd_io* io,
                 cudaStream_t s) {
