@@ -28,6 +28,9 @@ sys.path.insert(0, ROOT)
 METRIC = "FDTD Gcell-updates/s (400x400 TM, 2000 steps)"
 UNIT = "Gcell-updates/s"
 BYTES_PER_CELL_UPDATE = 28  # read+write Hx, Hy, Dz + read 1/eps (float32)
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_tm_tile launch on this
+# workload (ncu capture summarised in profiles/fdtd_tm_400x400_tile_kernel.md)
+TILE400_DRAM_BYTES_PER_LAUNCH = 3665280
 
 
 def _peaks():
@@ -265,10 +268,13 @@ def run_ours(args):
                        "parallelism": f"replicas x{ws}"},
             "gpu_launches": launches_per_run * args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "kernel": "k_tm_blocked<float>", "peak_kind": peak_kind,
-                         "note": "algorithmic 28 B/cell-update; 400x400 state is L2-resident "
-                                 "across the 8 time steps of a launch"},
+                         "frac": achieved / peak, "traffic": TILE400_DRAM_BYTES_PER_LAUNCH,
+                         "traffic_unit": "bytes per launch (8 time steps)",
+                         "algorithmic_bytes_per_launch": N * BYTES_PER_CELL_UPDATE * 8,
+                         "kernel": "k_tm_tile<float,32,48,8,512>", "peak_kind": peak_kind,
+                         "note": "algorithmic 28 B/cell-update; the 400x400 state is L2-resident "
+                                 "and each launch advances 8 steps in shared memory, so DRAM "
+                                 "traffic is ~10% of the algorithmic bytes"},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": "400x400 x %s FDTD steps, numpy FP64 oracle port"
                                        % os.environ.get("CEV_CPU_STEPS", "500")},

@@ -48,6 +48,27 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* smem /* NV*32
   }
 }
 
+// Block-wide sum of NV floats per thread: FP32 warp shuffles (the GB300 FP64
+// pipe is narrow), then the per-warp sums combined in FP64 by thread k < NV.
+// Result for value k in out[k] (valid in threads k < NV after the call).
+template <int NV>
+__device__ __forceinline__ void block_sum_f(float (&v)[NV], float* smem /* NV*32 */,
+                                            double (&out)[1], int k_of_thread) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_sumf(v[k]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = v[k];
+  __syncthreads();
+  double t = 0.0;
+  if (k_of_thread < NV)
+    for (int w = 0; w < nw; ++w) t += (double)smem[k_of_thread * 32 + w];
+  out[0] = t;
+}
+
 // Arrival counter: returns true in the whole block of the last block to
 // arrive (after its partials are visible).  Resets the counter.
 __device__ __forceinline__ bool last_block(unsigned* counter, unsigned nblocks) {
@@ -190,7 +211,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_multidot(DotArgs a) {
   const int nv = a.j + 1;
   const unsigned nblk = gridDim.x;
   const float2* w = a.V + ((size_t)(a.j + 1) * a.B + b) * a.n;
-  __shared__ double sm[2 * DOT_GROUP * 32];
+  __shared__ float smf[2 * DOT_GROUP * 32];
   double* part = a.ctx.partial + (size_t)b * a.ctx.part_stride;
   const size_t stride = (size_t)nblk * blockDim.x;
   for (int g0 = 0; g0 < nv; g0 += DOT_GROUP) {
@@ -208,34 +229,39 @@ __global__ void __launch_bounds__(RED_THREADS) k_multidot(DotArgs a) {
         }
       }
     }
-    double dv[2 * DOT_GROUP];
+    float fv[2 * DOT_GROUP];
 #pragma unroll
     for (int k = 0; k < DOT_GROUP; ++k) {
-      dv[2 * k] = acc[k].x;
-      dv[2 * k + 1] = acc[k].y;
+      fv[2 * k] = acc[k].x;
+      fv[2 * k + 1] = acc[k].y;
     }
-    block_sum<2 * DOT_GROUP>(dv, sm);
-    if (threadIdx.x == 0) {
-      for (int k = 0; k < DOT_GROUP && g0 + k < nv; ++k) {
-        part[(size_t)blockIdx.x * 2 * (a.m + 1) + 2 * (g0 + k)] = dv[2 * k];
-        part[(size_t)blockIdx.x * 2 * (a.m + 1) + 2 * (g0 + k) + 1] = dv[2 * k + 1];
-      }
-    }
+    double tot[1];
+    block_sum_f<2 * DOT_GROUP>(fv, smf, tot, threadIdx.x);
+    const int kk = threadIdx.x >> 1;
+    if (threadIdx.x < 2 * DOT_GROUP && g0 + kk < nv)
+      part[(size_t)blockIdx.x * 2 * (a.m + 1) + 2 * g0 + threadIdx.x] = tot[0];
     __syncthreads();
   }
   if (!last_block(a.ctx.counter + 2 * b, nblk)) return;
-  // fixed-order reduction over blocks, one vector k per thread
-  for (int k = threadIdx.x; k < nv; k += blockDim.x) {
+  // fixed-order reduction over blocks: one warp per vector, lanes stride the
+  // partials, then a shuffle tree (deterministic)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const size_t ps = 2 * (size_t)(a.m + 1);
+  for (int k = warp; k < nv; k += nw) {
     double re = 0.0, im = 0.0;
-    for (unsigned q = 0; q < nblk; ++q) {
-      re += __ldcg(part + (size_t)q * 2 * (a.m + 1) + 2 * k);
-      im += __ldcg(part + (size_t)q * 2 * (a.m + 1) + 2 * k + 1);
+    for (unsigned q = lane; q < nblk; q += 32) {
+      re += __ldcg(part + q * ps + 2 * k);
+      im += __ldcg(part + q * ps + 2 * k + 1);
     }
-    const double s = a.ctx.sc[(size_t)b * (a.m + 1) + k];
-    const double2 h = make_double2(s * re, s * im);
-    double2* Hc = a.ctx.H + ((size_t)b * a.m + a.j) * (a.m + 1);  // column j
-    a.ctx.hpass[(size_t)b * (a.m + 1) + k] = h;
-    Hc[k] = a.accumulate ? cadd(Hc[k], h) : h;
+    re = warp_sum(re);
+    im = warp_sum(im);
+    if (lane == 0) {
+      const double s = a.ctx.sc[(size_t)b * (a.m + 1) + k];
+      const double2 h = make_double2(s * re, s * im);
+      double2* Hc = a.ctx.H + ((size_t)b * a.m + a.j) * (a.m + 1);  // column j
+      a.ctx.hpass[(size_t)b * (a.m + 1) + k] = h;
+      Hc[k] = a.accumulate ? cadd(Hc[k], h) : h;
+    }
   }
 }
 
@@ -248,6 +274,9 @@ struct UpdArgs {
   KCtx ctx;
 };
 
+// Givens update of Hessenberg column j (FP64), run by the whole last block:
+// the column and the previous rotations are staged in shared memory so the
+// serial part touches no global memory.
 __device__ void givens_finish(const UpdArgs& a, int b, double hn) {
   KCtx& c = const_cast<KCtx&>(a.ctx);
   KState* st = c.st + b;
@@ -256,48 +285,63 @@ __device__ void givens_finish(const UpdArgs& a, int b, double hn) {
   double* cs = c.cs + (size_t)b * m;
   double2* sn = c.sn + (size_t)b * m;
   double2* gam = c.gam + (size_t)b * (m + 1);
-  Hc[j + 1] = make_double2(hn, 0.0);
-  for (int k = 0; k < j; ++k) {
-    const double2 h0 = Hc[k], h1 = Hc[k + 1];
-    // [c s; -conj(s) c] [h0; h1]
-    Hc[k] = cadd(cscale(h0, cs[k]), cmul(sn[k], h1));
-    Hc[k + 1] = csub(cscale(h1, cs[k]), cmulc(sn[k], h0));
+  __shared__ double2 sH[66];
+  __shared__ double2 sSn[64];
+  __shared__ double sCs[64];
+  for (int k = threadIdx.x; k <= j; k += blockDim.x) {
+    sH[k] = Hc[k];
+    if (k < j) {
+      sCs[k] = cs[k];
+      sSn[k] = sn[k];
+    }
   }
-  const double2 av = Hc[j];
-  const double aa = sqrt(av.x * av.x + av.y * av.y);
-  double cj;
-  double2 sj, rj;
-  if (aa == 0.0) {
-    cj = 0.0;
-    sj = make_double2(1.0, 0.0);
-    rj = make_double2(hn, 0.0);
-  } else {
-    const double t = sqrt(aa * aa + hn * hn);
-    cj = aa / t;
-    const double2 ph = make_double2(av.x / aa, av.y / aa);
-    sj = cscale(ph, hn / t);  // (a/|a|) conj(b)/t with b = hn real
-    rj = cscale(ph, t);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sH[j + 1] = make_double2(hn, 0.0);
+    for (int k = 0; k < j; ++k) {
+      const double2 h0 = sH[k], h1 = sH[k + 1];
+      // [c s; -conj(s) c] [h0; h1]
+      sH[k] = cadd(cscale(h0, sCs[k]), cmul(sSn[k], h1));
+      sH[k + 1] = csub(cscale(h1, sCs[k]), cmulc(sSn[k], h0));
+    }
+    const double2 av = sH[j];
+    const double aa = sqrt(av.x * av.x + av.y * av.y);
+    double cj;
+    double2 sj, rj;
+    if (aa == 0.0) {
+      cj = 0.0;
+      sj = make_double2(1.0, 0.0);
+      rj = make_double2(hn, 0.0);
+    } else {
+      const double t = sqrt(aa * aa + hn * hn);
+      cj = aa / t;
+      const double2 ph = make_double2(av.x / aa, av.y / aa);
+      sj = cscale(ph, hn / t);  // (a/|a|) conj(b)/t with b = hn real
+      rj = cscale(ph, t);
+    }
+    cs[j] = cj;
+    sn[j] = sj;
+    sH[j] = rj;
+    sH[j + 1] = make_double2(0.0, 0.0);
+    const double2 g = gam[j];
+    gam[j + 1] = cscale(cmulc(sj, g), -1.0);
+    gam[j] = cscale(g, cj);
+    const double2 gn = gam[j + 1];
+    const double res = sqrt(gn.x * gn.x + gn.y * gn.y);
+    st->res_est = res;
+    st->ncols = j + 1;
+    st->iters += 1;
+    const bool breakdown = !(hn > 1e-30);  // basis vectors have unit norm
+    c.sc[(size_t)b * (m + 1) + j + 1] = breakdown ? 0.0 : 1.0 / hn;
+    if (!isfinite(res) || !isfinite(hn)) {
+      st->nan = 1;
+      st->active = 0;
+    } else if (res <= st->thresh || breakdown || j + 1 >= m || st->iters >= c.max_iters) {
+      st->active = 0;
+    }
   }
-  cs[j] = cj;
-  sn[j] = sj;
-  Hc[j] = rj;
-  Hc[j + 1] = make_double2(0.0, 0.0);
-  const double2 g = gam[j];
-  gam[j + 1] = cscale(cmulc(sj, g), -1.0);
-  gam[j] = cscale(g, cj);
-  const double2 gn = gam[j + 1];
-  const double res = sqrt(gn.x * gn.x + gn.y * gn.y);
-  st->res_est = res;
-  st->ncols = j + 1;
-  st->iters += 1;
-  const bool breakdown = !(hn > 1e-30);  // basis vectors have unit norm
-  c.sc[(size_t)b * (m + 1) + j + 1] = breakdown ? 0.0 : 1.0 / hn;
-  if (!isfinite(res) || !isfinite(hn)) {
-    st->nan = 1;
-    st->active = 0;
-  } else if (res <= st->thresh || breakdown || j + 1 >= m || st->iters >= c.max_iters) {
-    st->active = 0;
-  }
+  __syncthreads();
+  for (int k = threadIdx.x; k <= j + 1; k += blockDim.x) Hc[k] = sH[k];
 }
 
 __global__ void __launch_bounds__(RED_THREADS) k_update(UpdArgs a) {
@@ -316,47 +360,69 @@ __global__ void __launch_bounds__(RED_THREADS) k_update(UpdArgs a) {
   const unsigned nblk = gridDim.x;
   const size_t stride = (size_t)nblk * blockDim.x;
   float nrm = 0.f;
+  constexpr int G = 8;  // basis vectors loaded together (predicated) per group
   for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
     float2 wv = w[n];
-    for (int k = 0; k < nv; ++k) {
-      const float2 v = a.V[((size_t)k * a.B + b) * a.n + n];
-      const float2 c = u[k];
-      wv.x -= v.x * c.x - v.y * c.y;
-      wv.y -= v.x * c.y + v.y * c.x;
+    for (int g0 = 0; g0 < nv; g0 += G) {
+      float2 v[G];
+#pragma unroll
+      for (int k = 0; k < G; ++k)
+        v[k] = (g0 + k < nv) ? a.V[((size_t)(g0 + k) * a.B + b) * a.n + n] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int k = 0; k < G; ++k) {
+        const float2 c = u[g0 + k < nv ? g0 + k : 0];
+        if (g0 + k < nv) {
+          wv.x -= v[k].x * c.x - v[k].y * c.y;
+          wv.y -= v[k].x * c.y + v[k].y * c.x;
+        }
+      }
     }
     w[n] = wv;
     nrm += wv.x * wv.x + wv.y * wv.y;
   }
   if (!a.final_pass) return;
   __shared__ double sm[32];
-  double acc[1] = {(double)nrm};
-  block_sum<1>(acc, sm);
+  __shared__ float smf[32];
+  float accf[1] = {nrm};
+  double tot[1];
+  block_sum_f<1>(accf, smf, tot, threadIdx.x);
   double* part = a.ctx.partial + (size_t)b * a.ctx.part_stride;
-  if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+  if (threadIdx.x == 0) part[blockIdx.x] = tot[0];
   if (!last_block(a.ctx.counter + 2 * b + 1, nblk)) return;
   double s[1] = {0.0};
   for (unsigned q = threadIdx.x; q < nblk; q += blockDim.x) s[0] += __ldcg(part + q);
   block_sum<1>(s, sm);
-  if (threadIdx.x == 0) givens_finish(a, b, sqrt(s[0]));
+  __shared__ double s_hn;
+  if (threadIdx.x == 0) s_hn = sqrt(s[0]);
+  __syncthreads();
+  givens_finish(a, b, s_hn);
 }
 
 // ------------------------------------------------- triangular solve + update
+// y = R^{-1} gamma for the k columns of this cycle, one block per problem:
+// R staged in shared memory, column-oriented back substitution.
 __global__ void k_trisolve(KCtx c, int B, int m) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= B) return;
-  KState* st = c.st + b;
+  const int b = blockIdx.x;
+  const KState* st = c.st + b;
   const int k = st->ncols;
+  if (k == 0) return;
+  // packed upper triangle: R[row][col] (row <= col) at col*(col+1)/2 + row
+  __shared__ double2 sR[64 * 65 / 2];
+  __shared__ double2 sT[64];
+  for (int col = 0; col < k; ++col)
+    for (int row = threadIdx.x; row <= col; row += blockDim.x)
+      sR[col * (col + 1) / 2 + row] = c.H[((size_t)b * m + col) * (m + 1) + row];
+  for (int r = threadIdx.x; r < k; r += blockDim.x) sT[r] = c.gam[(size_t)b * (m + 1) + r];
+  __syncthreads();
   double2* y = c.y + (size_t)b * m;
-  const double2* gam = c.gam + (size_t)b * (m + 1);
   for (int r = k - 1; r >= 0; --r) {
-    double2 t = gam[r];
-    for (int q = r + 1; q < k; ++q) {
-      const double2 h = c.H[((size_t)b * m + q) * (m + 1) + r];
-      t = csub(t, cmul(h, y[q]));
-    }
-    const double2 d = c.H[((size_t)b * m + r) * (m + 1) + r];
+    const double2 d = sR[r * (r + 1) / 2 + r];
     const double dd = d.x * d.x + d.y * d.y;
-    y[r] = dd > 0 ? cscale(cmulc(d, t), 1.0 / dd) : make_double2(0.0, 0.0);
+    const double2 yr = dd > 0 ? cscale(cmulc(d, sT[r]), 1.0 / dd) : make_double2(0.0, 0.0);
+    for (int q = threadIdx.x; q < r; q += blockDim.x)
+      sT[q] = csub(sT[q], cmul(sR[r * (r + 1) / 2 + q], yr));
+    if (threadIdx.x == 0) y[r] = yr;
+    __syncthreads();
   }
 }
 
@@ -387,9 +453,15 @@ __global__ void __launch_bounds__(RED_THREADS) k_xupdate(XupArgs a) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
     double2 acc = make_double2(0.0, 0.0);
-    for (int q = 0; q < k; ++q) {
-      const float2 v = base[((size_t)q * a.B + b) * a.n + n];
-      acc = cfma(cy[q], to_d(v), acc);
+    constexpr int G = 8;
+    for (int q0 = 0; q0 < k; q0 += G) {
+      float2 v[G];
+#pragma unroll
+      for (int q = 0; q < G; ++q)
+        v[q] = (q0 + q < k) ? base[((size_t)(q0 + q) * a.B + b) * a.n + n] : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int q = 0; q < G; ++q)
+        if (q0 + q < k) acc = cfma(cy[q0 + q], to_d(v[q]), acc);
     }
     // The cycle solved A' d = r with A' = scale*A and r the residual of
     // A' x = scale*b, so d is already a correction of x in SI units.
@@ -421,7 +493,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 int reduction_blocks(size_t n, int B) {
   const long target = 4L * sm_count();
   long nb = (target + B - 1) / B;
-  long cap = (long)((n + RED_THREADS * 4 - 1) / (RED_THREADS * 4));
+  long cap = (long)((n + RED_THREADS - 1) / RED_THREADS);
   return (int)std::max(1L, std::min(nb, cap));
 }
 
@@ -634,7 +706,7 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
       CEV_CHECK_LAUNCH("arnoldi step");
     }
     total_iters += m;
-    k_trisolve<<<(B + 63) / 64, 64, 0, s>>>(c, B, m);
+    k_trisolve<<<B, 64, 0, s>>>(c, B, m);
     XupArgs xa{N, B, m, flexible ? 1 : 0, V, Z, (double2*)xvec, 1.0, c};
     k_xupdate<<<rg, RED_THREADS, 0, s>>>(xa);
     CEV_CHECK_LAUNCH("cycle finish");
