@@ -67,6 +67,8 @@ SIGNATURES = {
     "cev_fdfd_fields": (I, [P, P, I, P, P, P, P]),
     "cev_fdfd_fields_adjoint": (I, [P, P, I, P, P, P, P, P, P]),
     "cev_fdfd_grad_eps": (I, [P, P, I, P, P, P, P]),
+    "cev_fdfd_jvp_rhs": (I, [P, P, I, P, P, P, P]),
+    "cev_fdfd_fields_jvp": (I, [P, P, I, P, P, P, P, P]),
     "cev_fdtd_plan_create": (I, [PP, I, I, D, I, I, I, P, P]),
     "cev_fdtd_plan_destroy": (I, [P]),
     "cev_fdtd_set_eps": (I, [P, P, P]),

@@ -53,8 +53,6 @@ def build(verbose=False, force=False, extra=()):
             obj = cmd[cmd.index("-o") + 1]
             if os.path.exists(obj):
                 os.remove(obj)
-            if os.path.exists(LIB):
-                os.remove(LIB)
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -64,6 +62,8 @@ def build(verbose=False, force=False, extra=()):
             print(r.stdout, r.stderr, flush=True)
         return r
 
+    if jobs and os.path.exists(LIB):
+        os.remove(LIB)  # a failed compile must not leave the previous library in place
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         list(ex.map(run, jobs))
     if jobs or force or not _newer(LIB, objs):

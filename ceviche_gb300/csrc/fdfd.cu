@@ -437,6 +437,108 @@ __global__ void k_grad_eps(GradArgs a) {
   }
 }
 
+
+// --------------------------------------------------------- forward mode
+// Tangent right-hand side rhs += -(dA/d eps . deps) x  (SI units):
+//   Ez: +eps0 w^2 deps x
+//   Hz: -(1/eps0)(Dxb (d'yy Dxf x) + Dyb (d'xx Dyf x)),
+//       d'yy = -dyy^2 (deps + deps[i-1,j])/2, d'xx = -dxx^2 (deps + deps[i,j-1])/2
+// Restates grad_sp_solve_entries_forward (ceviche/primitives.py:139-142), whose
+// sp_mult(g, indices, x) is dA.x for the entries tangent g, chained from eps.
+struct JvpArgs {
+  int nx, ny, batch, eps_shared, pol;
+  const double* eps;
+  const double* deps;
+  const double2* x;
+  double2* out;
+  const double2 *sfx, *sbx, *sfy, *sby;
+  double2 phx, phy;
+  const double* omega;
+  double dL;
+};
+
+__global__ void k_jvp_rhs(JvpArgs a) {
+  const size_t N = (size_t)a.nx * a.ny;
+  const int b = blockIdx.y;
+  const size_t ebs = a.eps_shared ? 0 : N;
+  const double* e = a.eps + b * ebs;
+  const double* de = a.deps + b * ebs;
+  const double2* x = a.x + b * N;
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < N;
+       n += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(n / a.ny), j = (int)(n % a.ny);
+    double2 v;
+    if (a.pol == POL_EZ) {
+      const double w = a.omega[b];
+      v = cscale(x[n], EPSILON_0 * w * w * de[n]);
+    } else {
+      const double2 *sfx = a.sfx + (size_t)b * a.nx, *sbx = a.sbx + (size_t)b * a.nx;
+      const double2 *sfy = a.sfy + (size_t)b * a.ny, *sby = a.sby + (size_t)b * a.ny;
+      // g_x(ii) = d'yy(ii,j) (Dxf x)(ii,j) ; g_y(jj) = d'xx(i,jj) (Dyf x)(i,jj)
+      auto gx = [&](int ii) {
+        const size_t m = (size_t)ii * a.ny + j;
+        const int ip = (ii + 1) % a.nx, im = (ii + a.nx - 1) % a.nx;
+        double2 xp = x[(size_t)ip * a.ny + j];
+        if (ii == a.nx - 1) xp = cmul(a.phx, xp);
+        const double2 df = cscale(cmul(sfx[ii], csub(xp, x[m])), 1.0 / a.dL);
+        const double d = hz_dd(e[m], e[(size_t)im * a.ny + j]);
+        return cscale(df, -d * d * 0.5 * (de[m] + de[(size_t)im * a.ny + j]));
+      };
+      auto gy = [&](int jj) {
+        const size_t m = (size_t)i * a.ny + jj;
+        const int jp = (jj + 1) % a.ny, jm = (jj + a.ny - 1) % a.ny;
+        double2 xp = x[(size_t)i * a.ny + jp];
+        if (jj == a.ny - 1) xp = cmul(a.phy, xp);
+        const double2 df = cscale(cmul(sfy[jj], csub(xp, x[m])), 1.0 / a.dL);
+        const double d = hz_dd(e[m], e[(size_t)i * a.ny + jm]);
+        return cscale(df, -d * d * 0.5 * (de[m] + de[(size_t)i * a.ny + jm]));
+      };
+      const int im = (i + a.nx - 1) % a.nx, jm = (j + a.ny - 1) % a.ny;
+      double2 gxm = gx(im), gym = gy(jm);
+      if (i == 0) gxm = cmul(cconj(a.phx), gxm);
+      if (j == 0) gym = cmul(cconj(a.phy), gym);
+      const double2 tx = cscale(cmul(sbx[i], csub(gx(i), gxm)), 1.0 / a.dL);
+      const double2 ty = cscale(cmul(sby[j], csub(gy(j), gym)), 1.0 / a.dL);
+      v = cscale(cadd(tx, ty), -1.0 / EPSILON_0);
+    }
+    a.out[b * N + n] = cadd(a.out[b * N + n], v);
+  }
+}
+
+// Direct eps tangent of the Hz field conversion (fdfd.py:150-162):
+// dEx += (-1j c) d'xx Dyf Hz ; dEy += (1j c) d'yy Dxf Hz, c = 1/(w eps0)
+__global__ void k_fields_jvp_hz(JvpArgs a, double2* df2) {
+  const size_t N = (size_t)a.nx * a.ny;
+  const int b = blockIdx.y;
+  const size_t ebs = a.eps_shared ? 0 : N;
+  const double* e = a.eps + b * ebs;
+  const double* de = a.deps + b * ebs;
+  const double2* u = a.x + b * N;
+  const double2* sfx = a.sfx + (size_t)b * a.nx;
+  const double2* sfy = a.sfy + (size_t)b * a.ny;
+  const double c = 1.0 / (a.omega[b] * EPSILON_0);
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < N;
+       n += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(n / a.ny), j = (int)(n % a.ny);
+    const int ip = (i + 1) % a.nx, im = (i + a.nx - 1) % a.nx;
+    const int jp = (j + 1) % a.ny, jm = (j + a.ny - 1) % a.ny;
+    double2 upx = u[(size_t)ip * a.ny + j], upy = u[(size_t)i * a.ny + jp];
+    if (i == a.nx - 1) upx = cmul(a.phx, upx);
+    if (j == a.ny - 1) upy = cmul(a.phy, upy);
+    const double2 dxf = cscale(cmul(sfx[i], csub(upx, u[n])), 1.0 / a.dL);
+    const double2 dyf = cscale(cmul(sfy[j], csub(upy, u[n])), 1.0 / a.dL);
+    const double dxx = hz_dd(e[n], e[(size_t)i * a.ny + jm]);
+    const double dyy = hz_dd(e[n], e[(size_t)im * a.ny + j]);
+    const double pxx = -dxx * dxx * 0.5 * (de[n] + de[(size_t)i * a.ny + jm]);
+    const double pyy = -dyy * dyy * 0.5 * (de[n] + de[(size_t)im * a.ny + j]);
+    // (-1j c) pxx dyf ; (1j c) pyy dxf
+    const double2 ex = make_double2(c * pxx * dyf.y, -c * pxx * dyf.x);
+    const double2 ey = make_double2(-c * pyy * dxf.y, c * pyy * dxf.x);
+    a.out[b * N + n] = cadd(a.out[b * N + n], ex);
+    df2[b * N + n] = cadd(df2[b * N + n], ey);
+  }
+}
+
 static dim3 grid_1d(size_t N, int batch) {
   const unsigned blocks = std::max(1u, std::min(ceil_div(N, 256), (unsigned)(8 * sm_count())));
   return dim3(blocks, batch, 1);
@@ -676,6 +778,31 @@ int cev_fdfd_grad_eps(cev_fdfd_plan p, const double* eps, int eps_shared, const 
   a.dL = p->dL;
   k_grad_eps<<<grid_1d(p->n(), eps_shared ? 1 : p->batch), 256, 0, s>>>(a);
   CEV_CHECK_LAUNCH("k_grad_eps");
+  return CEV_OK;
+}
+
+int cev_fdfd_jvp_rhs(cev_fdfd_plan p, const double* eps, int eps_shared, const double* deps,
+                     const void* x, void* rhs, cudaStream_t s) {
+  CEV_REQUIRE(p != nullptr, "plan is NULL");
+  CEV_REQUIRE(eps && deps && x && rhs, "NULL argument");
+  JvpArgs a{p->nx, p->ny, p->batch, eps_shared ? 1 : 0, p->pol, eps, deps, (const double2*)x,
+            (double2*)rhs, p->ft.sfx, p->ft.sbx, p->ft.sfy, p->ft.sby, p->phx, p->phy, p->omega_d,
+            p->dL};
+  k_jvp_rhs<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
+  CEV_CHECK_LAUNCH("k_jvp_rhs");
+  return CEV_OK;
+}
+
+int cev_fdfd_fields_jvp(cev_fdfd_plan p, const double* eps, int eps_shared, const double* deps,
+                        const void* fz, void* df1, void* df2, cudaStream_t s) {
+  CEV_REQUIRE(p != nullptr, "plan is NULL");
+  CEV_REQUIRE(eps && deps && fz && df1 && df2, "NULL argument");
+  if (p->pol == CEV_POL_EZ) return CEV_OK;  // Hx, Hy do not depend on eps directly
+  JvpArgs a{p->nx, p->ny, p->batch, eps_shared ? 1 : 0, p->pol, eps, deps, (const double2*)fz,
+            (double2*)df1, p->ft.sfx, p->ft.sbx, p->ft.sfy, p->ft.sby, p->phx, p->phy, p->omega_d,
+            p->dL};
+  k_fields_jvp_hz<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a, (double2*)df2);
+  CEV_CHECK_LAUNCH("k_fields_jvp_hz");
   return CEV_OK;
 }
 

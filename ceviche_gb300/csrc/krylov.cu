@@ -120,11 +120,14 @@ __global__ void __launch_bounds__(128) k_residual(ResArgs<POL> a) {
     float2* r = a.r + b * a.r_bs;
     const Coef<double> cyj = a.cy[(size_t)b * a.ny + j];
     const double bs = a.bscale;
+    // keep the complex64 copy O(1): a tiny right-hand side (e.g. an adjoint
+    // cotangent) would otherwise underflow float32
+    const double inv = 1.0 / st->rscale;
     auto ep = [&](int i, double2 v, double2) {
       const size_t n = (size_t)i * a.ny + j;
       const double2 bv = cscale(bb[n], bs);
       const double2 rv = csub(bv, v);
-      r[n] = to_f(rv);
+      r[n] = to_f(cscale(rv, inv));
       acc[0] += rv.x * rv.x + rv.y * rv.y;
       acc[1] += bv.x * bv.x + bv.y * bv.y;
     };
@@ -152,12 +155,40 @@ __global__ void __launch_bounds__(128) k_residual(ResArgs<POL> a) {
     st->res_est = beta;
     st->ncols = 0;
     const int m = a.m;
-    a.ctx.sc[(size_t)b * (m + 1)] = beta > 0 ? 1.0 / beta : 0.0;
+    a.ctx.sc[(size_t)b * (m + 1)] = beta > 0 ? st->rscale / beta : 0.0;
+    if (beta > 0) st->rscale = beta;
     a.ctx.gam[(size_t)b * (m + 1)] = make_double2(beta, 0.0);
     st->thresh = fmax(a.ctx.tol * st->bnorm * 0.5, a.ctx.inner_rtol * beta);
     const bool ok = isfinite(beta);
     if (!ok) st->nan = 1;
     st->active = (ok && beta > a.ctx.tol * st->bnorm && st->bnorm > 0) ? 1 : 0;
+  }
+}
+
+// ||scale*b|| in FP64 before the first residual; seeds rscale
+__global__ void __launch_bounds__(RED_THREADS) k_bnorm(const double2* bvec, double bscale, size_t n,
+                                                       KCtx c) {
+  const int b = blockIdx.y;
+  const unsigned nblk = gridDim.x;
+  const double2* bb = bvec + b * n;
+  double acc[1] = {0.0};
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x) {
+    const double2 v = cscale(bb[q], bscale);
+    acc[0] += v.x * v.x + v.y * v.y;
+  }
+  __shared__ double sm[32];
+  block_sum<1>(acc, sm);
+  double* part = c.partial + (size_t)b * c.part_stride;
+  if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+  if (!last_block(c.counter + 2 * b, nblk)) return;
+  double s[1] = {0.0};
+  for (unsigned q = threadIdx.x; q < nblk; q += blockDim.x) s[0] += __ldcg(part + q);
+  block_sum<1>(s, sm);
+  if (threadIdx.x == 0) {
+    const double bn = sqrt(s[0]);
+    c.st[b].bnorm = bn;
+    c.st[b].rscale = bn > 0 ? bn : 1.0;
   }
 }
 
@@ -652,7 +683,9 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
   std::vector<KState> hst(B);
   std::vector<double> best(B, INFINITY);
   std::vector<int> stall(B, 0), status(B, CEV_NOT_CONVERGED), cycles(B, 0);
-  if ((rc = residual(1)) != CEV_OK) return rc;
+  k_bnorm<<<rg, RED_THREADS, 0, s>>>((const double2*)bvec, p->scale, N, c);
+  CEV_CHECK_LAUNCH("k_bnorm");
+  if ((rc = residual(0)) != CEV_OK) return rc;
   int total_iters = 0;
   for (int cyc = 0;; ++cyc) {
     CEV_CUDA(cudaMemcpyAsync(hst.data(), c.st, sizeof(KState) * B, cudaMemcpyDeviceToHost, s));

@@ -17,6 +17,7 @@ struct KState {
   int nan;         // non-finite value seen
   int done;        // host decided the problem is finished
   int pad[3];
+  double rscale;   // the complex64 copy of the residual is stored divided by this
 };
 
 // Device pointers of the solver workspace.

@@ -7,8 +7,10 @@ as a float64 CUDA tensor.  The result is a numpy array of shape
 * reverse   -- one torch.autograd VJP per output element
                (jacobians.py:29-35); FDFD solves differentiate through the
                transposed GPU solve.
-* forward   -- the same Jacobian matrix, assembled from reverse-mode VJPs
-               (the GPU primitives do not define JVPs).
+* forward   -- one forward-mode JVP per input element
+               (torch.autograd.forward_ad; jacobians.py:38-51); FDFD solves
+               propagate tangents through one extra GPU solve each
+               (primitives.py:139-146).  Complex inputs follow jacobians.py:47-50.
 * numerical -- forward differences with ``step_size`` on the flattened input,
                exactly as jacobians.py:54-73.
 """
@@ -36,7 +38,7 @@ def jacobian(fun, argnum=0, mode="reverse", step_size=1e-6):
     if mode == "reverse":
         return _jacobian_reverse(fun, argnum)
     elif mode == "forward":
-        return _jacobian_reverse(fun, argnum)
+        return _jacobian_forward(fun, argnum)
     elif mode == "numerical":
         return _jacobian_numerical(fun, argnum, step_size=step_size)
     else:
@@ -60,6 +62,41 @@ def _jacobian_reverse(fun, argnum):
                                      allow_unused=True)
             rows.append(torch.zeros_like(x).reshape(-1) if g is None else g.reshape(-1))
         return _to_numpy(torch.stack(rows)).reshape(flat.numel(), x.numel())
+    return jac
+
+
+def _jacobian_forward(fun, argnum):
+    import torch.autograd.forward_ad as fwAD
+
+    def jac(*args):
+        x = _as_input(args[argnum])
+        n_in = x.numel()
+        a = list(args)
+
+        def column(t):
+            with fwAD.dual_level():
+                a[argnum] = fwAD.make_dual(x, t.reshape(x.shape))
+                out = fun(*a)
+                out = out if torch.is_tensor(out) else torch.as_tensor(out)
+                tan = fwAD.unpack_dual(out).tangent
+                if tan is None:
+                    tan = torch.zeros_like(out)
+                return tan.reshape(-1).detach()
+
+        cols = []
+        for i in range(n_in):
+            t = torch.zeros(n_in, dtype=x.dtype, device=x.device)
+            if x.is_complex():
+                t[i] = 1.0
+                re = column(t)
+                t[i] = 1j
+                im = column(t)
+                cols.append(re - 1j * im)
+            else:
+                t[i] = 1.0
+                cols.append(column(t))
+        J = torch.stack(cols, dim=1)
+        return _to_numpy(J)
     return jac
 
 

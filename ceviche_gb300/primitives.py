@@ -218,6 +218,30 @@ def fields_adjoint(plan, eps, fz, g1, g2, gz, geps):
                                       ptr(geps), stream_ptr()), "fields_adjoint")
 
 
+def jvp_rhs(plan, eps, deps, x, rhs):
+    """rhs += -(dA/d eps . deps) x (in place)."""
+    lib = _lib.load()
+    e, sh = _eps_arg(plan, eps, torch.float64)
+    de, _ = _eps_arg(plan, deps, torch.float64)
+    if de.shape != e.shape:
+        de = de.expand_as(e).contiguous()
+    xt = _field_arg(plan, x, torch.complex128)
+    check(lib.cev_fdfd_jvp_rhs(plan.handle, ptr(e), sh, ptr(de), ptr(xt), ptr(rhs), stream_ptr()),
+          "jvp_rhs")
+
+
+def fields_jvp(plan, eps, deps, fz, df1, df2):
+    """(df1, df2) += direct eps tangent of the secondary fields (Hz only)."""
+    lib = _lib.load()
+    e, sh = _eps_arg(plan, eps, torch.float64)
+    de, _ = _eps_arg(plan, deps, torch.float64)
+    if de.shape != e.shape:
+        de = de.expand_as(e).contiguous()
+    z = _field_arg(plan, fz, torch.complex128)
+    check(lib.cev_fdfd_fields_jvp(plan.handle, ptr(e), sh, ptr(de), ptr(z), ptr(df1), ptr(df2),
+                                  stream_ptr()), "fields_jvp")
+
+
 def grad_eps(plan, eps, x, mu, geps):
     """geps += system-matrix part of dL/d(eps) given x and mu = A^-T conj(g_x)."""
     lib = _lib.load()
@@ -247,6 +271,7 @@ class FDFDSolve(torch.autograd.Function):
         ctx.src_shape = src.shape
         ctx.eps_shape = eps.shape
         ctx.save_for_backward(eps, x)
+        ctx.save_for_forward(eps, x)
         ctx.info = info
         return f1, f2, x
 
@@ -275,3 +300,19 @@ class FDFDSolve(torch.autograd.Function):
             grad_src = gs.real if ctx.src_real else gs
             grad_src = grad_src.reshape(ctx.src_shape)
         return geps_out, grad_src, None, None
+
+    @staticmethod
+    def jvp(ctx, deps, dsrc, _plan, _opts):
+        """Tangent solve A dx = 1j w dsrc - dA x (primitives.py:139-146)."""
+        plan = ctx.plan
+        eps, x = ctx.saved_tensors
+        rhs = torch.zeros_like(x)
+        if dsrc is not None:
+            rhs += 1j * plan.omega_t.view(-1, 1, 1) * _field_arg(plan, dsrc, torch.complex128)
+        if deps is not None:
+            jvp_rhs(plan, eps, deps, x, rhs)
+        dx, _ = solve(plan, eps, rhs, **ctx.opts)
+        df1, df2 = fields(plan, eps, dx)
+        if deps is not None:
+            fields_jvp(plan, eps, deps, x, df1, df2)
+        return df1, df2, dx

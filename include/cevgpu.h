@@ -164,6 +164,25 @@ CEV_API int cev_fdfd_fields_adjoint(cev_fdfd_plan plan, const double* eps, int e
 CEV_API int cev_fdfd_grad_eps(cev_fdfd_plan plan, const double* eps, int eps_shared, const void* x,
                       const void* mu, double* geps, cudaStream_t stream);
 
+/*
+ * Forward mode (JVP).  rhs += -(dA/d eps . deps) x, the right-hand side of the
+ * tangent solve A dx = i w dsrc - dA x.  Restates
+ * grad_sp_solve_entries_forward / grad_sp_mult_entries_forward
+ * (ceviche/primitives.py:90-98, 139-146) chained from eps through
+ * fdfd.py:179 (Ez) and fdfd.py:211-233 (Hz).  deps has the layout of eps.
+ */
+CEV_API int cev_fdfd_jvp_rhs(cev_fdfd_plan plan, const double* eps, int eps_shared,
+                             const double* deps, const void* x, void* rhs, cudaStream_t stream);
+
+/*
+ * Direct eps tangent of the secondary fields: (df1, df2) += d(F1, F2)/d eps . deps
+ * at fixed Fz.  Zero for Ez; for Hz the 1/(eps_avg + 1e-5) factors of
+ * fdfd.py:150-162.  The full tangent adds cev_fdfd_fields(dFz).
+ */
+CEV_API int cev_fdfd_fields_jvp(cev_fdfd_plan plan, const double* eps, int eps_shared,
+                                const double* deps, const void* fz, void* df1, void* df2,
+                                cudaStream_t stream);
+
 /* ============================== FDTD ==================================== */
 
 typedef struct cev_fdtd_plan_s* cev_fdtd_plan;

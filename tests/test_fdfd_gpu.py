@@ -181,3 +181,49 @@ def test_solver_reports_nonconvergence(cev):
     assert info[0]["code"] == 1
     with pytest.raises(Exception):
         P.solve(plan, torch.as_tensor(p["eps"]), b, max_iters=5, restart=5, strict=True)
+
+
+@pytest.mark.parametrize("pol", ["ez", "hz"])
+def test_forward_mode_jacobian(cev, pol):
+    """jacobian(mode='forward') through the GPU tangent solve equals reverse
+    mode and numerical differences (test_gradients_fdfd.py:106-132, 164-190)."""
+    rng = np.random.default_rng(4)
+    Nx, Ny = 12, 10
+    omega, dL, npml = 2 * np.pi * 200e12, 1e-6, [3, 3]
+    eps0 = rng.random((Nx, Ny)) + 1
+    src = np.zeros((Nx, Ny))
+    src[6, 5] = 1.0
+    cls = cev.fdfd_ez if pol == "ez" else cev.fdfd_hz
+    F = cls(omega, dL, eps0, npml, tol=1e-11)
+    srct = torch.as_tensor(src, device="cuda")
+
+    def J(e):
+        F.eps_r = e.reshape(Nx, Ny)
+        f1, f2, fz = F.solve(F.eps_r * srct)
+        return torch.stack([(fz.abs() ** 2).sum(), (f1.abs() ** 2).sum() + (f2.abs() ** 2).sum()])
+
+    gf = cev.jacobian(J, mode="forward")(eps0.ravel())
+    gr = cev.jacobian(J, mode="reverse")(eps0.ravel())
+    gn = cev.jacobian(J, mode="numerical", step_size=1e-6)(eps0.ravel())
+    assert gf.shape == gr.shape == (2, Nx * Ny)
+    assert np.linalg.norm(gf - gr) / np.linalg.norm(gr) < 1e-8
+    assert np.linalg.norm(gn - gf) / np.linalg.norm(gn) < 1e-4
+
+
+@pytest.mark.parametrize("pol", ["ez", "hz"])
+@pytest.mark.parametrize("mag", [1e-30, 1e20])
+def test_solve_extreme_rhs_magnitudes(cev, pol, mag):
+    """Right-hand sides far outside float32 range after non-dimensionalisation
+    (e.g. adjoint cotangents of tiny fields) still solve to tolerance."""
+    from ceviche_gb300 import primitives as P
+    rng = np.random.default_rng(8)
+    Nx, Ny, dL, npml, om = 24, 20, 1e-6, [4, 4], 2 * np.pi * 200e12
+    eps = 1 + rng.random((Nx, Ny))
+    b = mag * (rng.standard_normal((Nx, Ny)) + 1j * rng.standard_normal((Nx, Ny)))
+    plan = P.get_plan(pol, (Nx, Ny), dL, om, npml)
+    for tr in (False, True):
+        x, info = P.solve(plan, torch.as_tensor(eps), torch.as_tensor(b), transpose=tr, tol=1e-9)
+        A = ofd.make_A(pol, om, dL, eps, npml)
+        A = A.T if tr else A
+        assert info[0]["code"] == 0
+        assert ofd.true_residual(A, x.cpu().numpy().ravel(), b.ravel()) < 1e-9
