@@ -78,6 +78,7 @@ SIGNATURES = {
     "cev_fdtd_run_tm": (I, [P, C.POINTER(FDTDState), I, C.POINTER(FDTDIO), P]),
     "cev_fdtd_run_tm_noalloc": (I, [I, I, D, I, I, P, C.POINTER(FDTDState), I, C.POINTER(FDTDIO),
                                     P]),
+    "cev_fdtd_step_adjoint_tm": (I, [P, P, P, P, C.POINTER(FDTDState), P, P, P]),
     "cev_fdtd_adjoint_workspace_size": (S, [P, I, I]),
     "cev_fdtd_adjoint_tm": (I, [P, I, I, C.POINTER(FDTDIO), P, P, P, S, P]),
 }

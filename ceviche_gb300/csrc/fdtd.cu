@@ -661,6 +661,17 @@ __global__ void k_adj_c(AdjArgs<R> a, const R* dz_prev, double* geps, int np, co
   if (dz_prev) geps[n] += (double)aez * (double)(-dz_prev[n] * ie * ie);
 }
 
+// gradient of an output Ez^n = Dz^n / eps: aDz^n += g iez ; geps += g (-Dz^n iez^2)
+template <typename R>
+__global__ void k_adj_out_ez(int N, R* adz, const R* gez, const R* dz, const R* iez, double* geps) {
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < (size_t)N;
+       n += (size_t)gridDim.x * blockDim.x) {
+    const R g = gez[n], ie = iez[n];
+    adz[n] += g * ie;
+    geps[n] += (double)g * (double)(-dz[n] * ie * ie);
+  }
+}
+
 // initial adjoint for the last output step T: aEz^T = w_T p
 template <typename R>
 __global__ void k_adj_init(int N, R* adz, const R* iez, double* geps, const R* dz_T, int np,
@@ -709,6 +720,33 @@ int step_impl(cev_fdtd_plan p, const cev_fdtd_state* st, const R* jx, const R* j
   }
   k_tm_d<R><<<g, blk, 0, s>>>(a);
   CEV_CHECK_LAUNCH("fdtd step");
+  return CEV_OK;
+}
+
+
+template <typename R>
+int step_adjoint_impl(cev_fdtd_plan p, const R* dz_in, const R* dz_out, const R* gez,
+                      const cev_fdtd_state* adj, R* scratch, double* geps, cudaStream_t s) {
+  const size_t N = p->n();
+  AdjArgs<R> a;
+  a.nx = p->nx; a.ny = p->ny;
+  a.ahx = (R*)adj->hx; a.ahy = (R*)adj->hy; a.adz = (R*)adj->dz;
+  a.aicex = (R*)adj->icex; a.aicey = (R*)adj->icey; a.aidz = (R*)adj->idz;
+  a.ach = scratch; a.adey = scratch + N; a.adex = scratch + 2 * N; a.adzp = scratch + 3 * N;
+  a.iez = (const R*)p->iez;
+  a.ax = (const AxisCoef<R>*)p->ax;
+  a.ay = (const AxisCoef<R>*)p->ay;
+  a.S = (R)p->S;
+  if (gez) {
+    const unsigned g1 = std::max(1u, std::min(ceil_div(N, 256), 8u * sm_count()));
+    k_adj_out_ez<R><<<g1, 256, 0, s>>>((int)N, a.adz, gez, dz_out, a.iez, geps);
+  }
+  const dim3 blk(32, 8);
+  const dim3 g = grid2(p->nx, p->ny, blk);
+  k_adj_a<R><<<g, blk, 0, s>>>(a);
+  k_adj_b<R><<<g, blk, 0, s>>>(a);
+  k_adj_c<R><<<g, blk, 0, s>>>(a, dz_in, geps, 0, nullptr, nullptr);
+  CEV_CHECK_LAUNCH("fdtd step adjoint");
   return CEV_OK;
 }
 
@@ -991,6 +1029,20 @@ int cev_fdtd_run_tm(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const
   if (nsteps == 0) return CEV_OK;
   if (p->prec == CEV_PREC_C128) return run_tm_impl<double>(p, st, nsteps, io, s);
   return run_tm_impl<float>(p, st, nsteps, io, s);
+}
+
+int cev_fdtd_step_adjoint_tm(cev_fdtd_plan p, const void* dz_in, const void* dz_out,
+                             const void* g_ez, const cev_fdtd_state* adj, void* scratch,
+                             double* geps, cudaStream_t s) {
+  CEV_REQUIRE(p && dz_in && adj && scratch && geps, "NULL argument");
+  CEV_REQUIRE(adj->hx && adj->hy && adj->dz && adj->icex && adj->icey && adj->idz,
+              "adjoint state incomplete");
+  CEV_REQUIRE(!g_ez || dz_out, "g_ez needs dz_out");
+  if (p->prec == CEV_PREC_C128)
+    return step_adjoint_impl<double>(p, (const double*)dz_in, (const double*)dz_out,
+                                     (const double*)g_ez, adj, (double*)scratch, geps, s);
+  return step_adjoint_impl<float>(p, (const float*)dz_in, (const float*)dz_out, (const float*)g_ez,
+                                  adj, (float*)scratch, geps, s);
 }
 
 size_t cev_fdtd_adjoint_workspace_size(cev_fdtd_plan p, int nsteps, int C) {

@@ -125,6 +125,15 @@ class fdtd:
         zero3 = torch.zeros((self.Nx, self.Ny, 1), dtype=self.dtype, device="cuda")
         self.fields = {k: zero3 for k in ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Hx", "Hy", "Hz")}
 
+    def _iez(self):
+        ez = torch.empty((self.Nx, self.Ny), dtype=self.dtype, device="cuda")
+        one = torch.ones((self.Nx, self.Ny), dtype=self.dtype, device="cuda")
+        st = _lib.FDTDState()
+        st.dz = one.data_ptr()
+        check(_lib.load().cev_fdtd_e_fields(self._plan_h, C.byref(st), None, None, ptr(ez),
+                                            stream_ptr()), "fdtd_e_fields")
+        return ez
+
     def _state(self):
         s = _lib.FDTDState()
         for k, v in self._st.items():
@@ -141,9 +150,25 @@ class fdtd:
         t = t.to(device="cuda", dtype=self.dtype).reshape(self.Nx, self.Ny).contiguous()
         return t
 
+    def _differentiable(self, *srcs):
+        e = self._eps_r
+        need = (torch.is_tensor(e) and e.requires_grad) or any(
+            torch.is_tensor(j) and j.requires_grad for j in srcs if j is not None)
+        return need and torch.is_grad_enabled()
+
     def forward(self, Jx=None, Jy=None, Jz=None):
-        """One time step of FDTD (ceviche/fdtd.py:74-144)."""
+        """One time step of FDTD (ceviche/fdtd.py:74-144).
+
+        When eps_r (or Jz) is a tensor that requires grad, the TM step is
+        recorded for autograd (state advanced out of place; backward is the
+        per-step adjoint kernel), so objectives summed over steps can be
+        differentiated as in the reference's gradient tests.
+        """
         lib = _lib.load()
+        if self._differentiable(Jx, Jy, Jz):
+            if Jx is not None or Jy is not None:
+                raise NotImplementedError("differentiable steps support the TM (Jz) source only")
+            return self._forward_autograd(Jz)
         self.t_index += 1
         jx, jy, jz = self._src(Jx), self._src(Jy), self._src(Jz)
         if (jx is not None or jy is not None) and self._te is None:
@@ -166,6 +191,22 @@ class fdtd:
         if self._te is not None:
             f["Hz"], f["Dx"], f["Dy"] = v3(self._te["hz"]), v3(self._te["dx"]), v3(self._te["dy"])
             f["Ex"], f["Ey"] = v3(ex), v3(ey)
+        return f
+
+    def _forward_autograd(self, Jz):
+        self.t_index += 1
+        eps = self._eps_r
+        jz = None
+        if Jz is not None:
+            jz = Jz if torch.is_tensor(Jz) else torch.as_tensor(np.asarray(Jz))
+            jz = jz.to(device="cuda", dtype=self.dtype).reshape(self.Nx, self.Ny)
+        st = [self._st[k] for k in _TM]
+        out = _TMStep.apply(eps, jz, self, *st)
+        for k, v in zip(_TM, out[:6]):
+            self._st[k] = v
+        v3 = lambda t: t.view(self.Nx, self.Ny, 1)
+        f = self.fields
+        f["Hx"], f["Hy"], f["Dz"], f["Ez"] = v3(out[0]), v3(out[1]), v3(out[2]), v3(out[6])
         return f
 
     # -- bulk TM runner
@@ -213,6 +254,53 @@ class fdtd:
         self.fields.update(Hx=v3(self._st["hx"]), Hy=v3(self._st["hy"]), Dz=v3(self._st["dz"]),
                            Ez=v3(ez))
         return out
+
+
+class _TMStep(torch.autograd.Function):
+    """One TM step, out of place: (eps, jz, state) -> (new state, Ez)."""
+
+    @staticmethod
+    def forward(ctx, eps, jz, F, hx, hy, dz, icex, icey, idz):
+        lib = _lib.load()
+        new = [t.clone() for t in (hx, hy, dz, icex, icey, idz)]
+        st = _lib.FDTDState()
+        for k, v in zip(_TM, new):
+            setattr(st, k, v.data_ptr())
+        jzc = None if jz is None else jz.detach().contiguous()
+        check(lib.cev_fdtd_step(F._plan_h, C.byref(st), None, None, ptr(jzc), 0, stream_ptr()),
+              "fdtd_step")
+        ez = torch.empty_like(new[2])
+        check(lib.cev_fdtd_e_fields(F._plan_h, C.byref(st), None, None, ptr(ez), stream_ptr()),
+              "fdtd_e_fields")
+        ctx.F = F
+        ctx.eps_shape = eps.shape if torch.is_tensor(eps) else None
+        ctx.has_jz = jz is not None
+        ctx.save_for_backward(dz, new[2])
+        return (*new, ez)
+
+    @staticmethod
+    def backward(ctx, ghx, ghy, gdz, gicex, gicey, gidz, gez):
+        F = ctx.F
+        lib = _lib.load()
+        dz_in, dz_out = ctx.saved_tensors
+        z = lambda g: torch.zeros_like(dz_in) if g is None else g.detach().contiguous().clone()
+        adj = [z(g) for g in (ghx, ghy, gdz, gicex, gicey, gidz)]
+        gjz = None
+        if ctx.has_jz and ctx.needs_input_grad[1]:
+            gjz = adj[2] + (0 if gez is None else gez * F._iez())
+        st = _lib.FDTDState()
+        for k, v in zip(_TM, adj):
+            setattr(st, k, v.data_ptr())
+        scratch = torch.empty(4 * F.Nx * F.Ny, dtype=F.dtype, device="cuda")
+        geps = torch.zeros((F.Nx, F.Ny), dtype=torch.float64, device="cuda")
+        gezc = None if gez is None else gez.detach().contiguous()
+        check(lib.cev_fdtd_step_adjoint_tm(F._plan_h, ptr(dz_in.contiguous()), ptr(dz_out),
+                                           ptr(gezc), C.byref(st), ptr(scratch), ptr(geps),
+                                           stream_ptr()), "fdtd_step_adjoint_tm")
+        ge = None
+        if ctx.eps_shape is not None and ctx.needs_input_grad[0]:
+            ge = geps.reshape(ctx.eps_shape)
+        return (ge, gjz, None, *adj)
 
 
 class _ProbeSeries(torch.autograd.Function):

@@ -265,6 +265,20 @@ CEV_API int cev_fdtd_run_tm_noalloc(int nx, int ny, double dL, int npml_x, int n
                                     const double* eps, const cev_fdtd_state* st, int nsteps,
                                     const cev_fdtd_io* io, cudaStream_t stream);
 
+/*
+ * Reverse of ONE TM step of cev_fdtd_step.  On entry adj holds dL/d(state after the step) (hx, hy, dz, icex, icey, idz)
+ * and g_ez (optional, with dz_out = Dz after the step) dL/dEz after the step;
+ * on return adj holds dL/d(state before the step) and geps (double [nx][ny])
+ * has the step's eps term added.  dz_in = Dz before the step.  scratch: 4*nx*ny
+ * elements of the field precision.  The step's source gradient dL/dJz is
+ * the gradient of Dz after the step (g_dz + g_ez/eps), which the caller forms
+ * before the call.  This is the per-step VJP that autograd tapes through
+ * ceviche/fdtd.py:74-144 for test_gradients_fdtd.py:66-165.
+ */
+CEV_API int cev_fdtd_step_adjoint_tm(cev_fdtd_plan plan, const void* dz_in, const void* dz_out,
+                                     const void* g_ez, const cev_fdtd_state* adj, void* scratch,
+                                     double* geps, cudaStream_t stream);
+
 /* Workspace bytes for cev_fdtd_adjoint_tm. */
 CEV_API size_t cev_fdtd_adjoint_workspace_size(cev_fdtd_plan plan, int nsteps, int ckpt_every);
 

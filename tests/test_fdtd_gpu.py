@@ -172,3 +172,27 @@ def test_every_tile_configuration(cev, tile, monkeypatch):
     assert _rel(series, np.array(ref)) < 1e-6
     for k in ("Ez", "Hx", "Hy", "Dz"):
         assert _rel(_np(A.fields[k]), _np(B.fields[k])) < 1e-6
+
+
+@pytest.mark.parametrize("precision,tol", [("float64", 1e-8), ("float32", 2e-4)])
+def test_per_step_autograd_like_reference_test(cev, precision, tol):
+    """The reference gradient test pattern (test_gradients_fdtd.py:66-88):
+    jacobian over a Python loop of F.forward(Jz=...) summing E each step,
+    against the reference's central differences."""
+    d = np.load(os.path.join(GOLDEN, "grad_fd.npz"))
+    eps0, prof, amps = d["fdtd_eps"], d["fdtd_prof"], d["fdtd_amps"]
+    Nx, Ny = eps0.shape
+    F = cev.fdtd(eps0[:, :, None], dL=5e-8, npml=[2, 2, 0], precision=precision)
+    src = torch.as_tensor(prof[:, :, None], device="cuda")
+
+    def objective(eps_arr):
+        F.eps_r = eps_arr.reshape((Nx, Ny, 1))
+        S = 0.0
+        for t in range(len(amps)):
+            fields = F.forward(Jz=src * float(amps[t]))
+            S = S + torch.sum(fields["Ex"] + fields["Ey"] + fields["Ez"])
+        return S
+
+    jac = cev.jacobian(objective, mode="reverse")(eps0.ravel())
+    assert jac.shape == (1, Nx * Ny)
+    assert _rel(jac.ravel(), d["fdtd_grad"]) < tol
