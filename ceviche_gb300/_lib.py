@@ -69,6 +69,12 @@ SIGNATURES = {
     "cev_fdfd_grad_eps": (I, [P, P, I, P, P, P, P]),
     "cev_fdfd_jvp_rhs": (I, [P, P, I, P, P, P, P]),
     "cev_fdfd_fields_jvp": (I, [P, P, I, P, P, P, P, P]),
+    "cev_fdfd_mf_plan_create": (I, [PP, I, I, D, D, D, I, I, I, D, D]),
+    "cev_fdfd_mf_apply": (I, [P, P, I, P, P, P, I, P]),
+    "cev_fdfd_mf_solve_workspace_size": (S, [P, I, C.POINTER(SolveOpts)]),
+    "cev_fdfd_mf_solve": (I, [P, P, I, P, P, P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), P, S,
+                              P]),
+    "cev_fdfd_mf_grad": (I, [P, I, P, P, P, P, P]),
     "cev_fdtd_plan_create": (I, [PP, I, I, D, I, I, I, P, P]),
     "cev_fdtd_plan_destroy": (I, [P]),
     "cev_fdtd_set_eps": (I, [P, P, P]),

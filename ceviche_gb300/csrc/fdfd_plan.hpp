@@ -48,5 +48,7 @@ struct cev_fdfd_plan_s {
   double* omega_d = nullptr;  // [batch]
   cev::FieldTab ft;
   double2 phx, phy;  // Bloch phasors exp(1j*bloch)
+  int mf_nsb = -1;      // multi-frequency plan: sidebands on each side (-1: not one)
+  double omega_mod = 0;
   size_t n() const { return (size_t)nx * ny; }
 };

@@ -14,76 +14,18 @@
 // reads the FP64 residuals once per cycle.
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <vector>
 
 #include "fdfd_plan.hpp"
 #include "krylov.hpp"
+#include "reduce.cuh"
 
 namespace cev {
 
 void launch_geometry(int nx, int ny, int batch, dim3& grid, dim3& block, int& rows);
 
-static constexpr int RED_THREADS = 256;
 static constexpr int DOT_GROUP = 16;
-
-// --------------------------------------------------------------- reductions
-// Block-wide sum of NV doubles per thread into out (valid in thread 0).
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV], double* smem /* NV*32 */) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
-  __syncthreads();
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = v[k];
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      double t = lane < nw ? smem[k * 32 + lane] : 0.0;
-      v[k] = warp_sum(t);
-    }
-  }
-}
-
-// Block-wide sum of NV floats per thread: FP32 warp shuffles (the GB300 FP64
-// pipe is narrow), then the per-warp sums combined in FP64 by thread k < NV.
-// Result for value k in out[k] (valid in threads k < NV after the call).
-template <int NV>
-__device__ __forceinline__ void block_sum_f(float (&v)[NV], float* smem /* NV*32 */,
-                                            double (&out)[1], int k_of_thread) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int k = 0; k < NV; ++k) v[k] = warp_sumf(v[k]);
-  __syncthreads();
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < NV; ++k) smem[k * 32 + warp] = v[k];
-  __syncthreads();
-  double t = 0.0;
-  if (k_of_thread < NV)
-    for (int w = 0; w < nw; ++w) t += (double)smem[k_of_thread * 32 + w];
-  out[0] = t;
-}
-
-// Arrival counter: returns true in the whole block of the last block to
-// arrive (after its partials are visible).  Resets the counter.
-__device__ __forceinline__ bool last_block(unsigned* counter, unsigned nblocks) {
-  __shared__ bool s_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    const unsigned t = atomicAdd(counter, 1u);
-    s_last = (t == nblocks - 1);
-    if (s_last) *counter = 0u;
-  }
-  __syncthreads();
-  if (s_last) __threadfence();
-  return s_last;
-}
 
 // --------------------------------------------------------------- residual
 template <int POL>
@@ -111,7 +53,7 @@ __global__ void __launch_bounds__(128) k_residual(ResArgs<POL> a) {
   const size_t N = (size_t)a.nx * a.ny;
   const unsigned nblk = gridDim.x * gridDim.y;
   const unsigned blk = blockIdx.y * gridDim.x + blockIdx.x;
-  double acc[2] = {0.0, 0.0};
+  double acc[1] = {0.0};
   if (j < a.ny) {
     const int i0 = blockIdx.y * a.rows;
     const int i1 = min(i0 + a.rows, a.nx);
@@ -129,40 +71,11 @@ __global__ void __launch_bounds__(128) k_residual(ResArgs<POL> a) {
       const double2 rv = csub(bv, v);
       r[n] = to_f(cscale(rv, inv));
       acc[0] += rv.x * rv.x + rv.y * rv.y;
-      acc[1] += bv.x * bv.x + bv.y * bv.y;
     };
     stencil_column<double, POL>(a.nx, a.ny, j, i0, i1, x, a.eps + b * a.eps_bs,
                                 a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
   }
-  __shared__ double sm[2 * 32];
-  block_sum<2>(acc, sm);
-  double* part = a.ctx.partial + (size_t)b * a.ctx.part_stride;
-  if (threadIdx.x == 0) {
-    part[2 * blk] = acc[0];
-    part[2 * blk + 1] = acc[1];
-  }
-  if (!last_block(a.ctx.counter + 2 * b, nblk)) return;
-  double s[2] = {0.0, 0.0};
-  for (unsigned k = threadIdx.x; k < nblk; k += blockDim.x) {
-    s[0] += __ldcg(part + 2 * k);
-    s[1] += __ldcg(part + 2 * k + 1);
-  }
-  block_sum<2>(s, sm);
-  if (threadIdx.x == 0) {
-    const double beta = sqrt(s[0]);
-    if (a.first) st->bnorm = sqrt(s[1]);
-    st->beta = beta;
-    st->res_est = beta;
-    st->ncols = 0;
-    const int m = a.m;
-    a.ctx.sc[(size_t)b * (m + 1)] = beta > 0 ? st->rscale / beta : 0.0;
-    if (beta > 0) st->rscale = beta;
-    a.ctx.gam[(size_t)b * (m + 1)] = make_double2(beta, 0.0);
-    st->thresh = fmax(a.ctx.tol * st->bnorm * 0.5, a.ctx.inner_rtol * beta);
-    const bool ok = isfinite(beta);
-    if (!ok) st->nan = 1;
-    st->active = (ok && beta > a.ctx.tol * st->bnorm && st->bnorm > 0) ? 1 : 0;
-  }
+  residual_finish(acc[0], a.ctx, b, a.m, nblk, blk);
 }
 
 // ||scale*b|| in FP64 before the first residual; seeds rscale
@@ -513,12 +426,6 @@ __global__ void k_zero_c128(double2* x, size_t n) {
 }
 
 // ----------------------------------------------------------- workspace
-struct Layout {
-  size_t eps32, V, Z, partial, counter, st, H, cs, sn, gam, sc, y, hpass, pc, total;
-  size_t part_stride;
-  int nblk;
-};
-
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 int reduction_blocks(size_t n, int B) {
@@ -528,23 +435,19 @@ int reduction_blocks(size_t n, int B) {
   return (int)std::max(1L, std::min(nb, cap));
 }
 
-static Layout layout(const cev_fdfd_plan_s* p, const cev_solve_opts& o) {
-  Layout L{};
-  const size_t N = p->n();
-  const int B = p->batch, m = o.restart;
-  dim3 g, bl;
-  int rows;
-  launch_geometry(p->nx, p->ny, B, g, bl, rows);
-  const size_t res_blocks = (size_t)g.x * g.y;
+KLayout klayout(const KrylovProblem& P, const cev_solve_opts& o, size_t pc_bytes) {
+  KLayout L{};
+  const size_t N = P.n;
+  const int B = P.B, m = o.restart;
   L.nblk = reduction_blocks(N, B);
-  L.part_stride = std::max((size_t)L.nblk * 2 * (m + 1), res_blocks * 2);
+  L.part_stride = std::max((size_t)L.nblk * 2 * (m + 1), P.res_blocks);
   size_t off = 0;
   auto take = [&](size_t bytes) {
     size_t at = off;
     off = align256(off + bytes);
     return at;
   };
-  L.eps32 = take(sizeof(float) * N * B);
+  L.extra = take(P.extra_bytes);
   L.V = take(sizeof(float2) * N * B * (m + 1));
   L.Z = take(o.precond != CEV_PRECOND_NONE ? sizeof(float2) * N * B * m : 0);
   L.partial = take(sizeof(double) * L.part_stride * B);
@@ -558,59 +461,32 @@ static Layout layout(const cev_fdfd_plan_s* p, const cev_solve_opts& o) {
   L.y = take(sizeof(double2) * (size_t)B * m);
   L.hpass = take(sizeof(double2) * (size_t)B * (m + 1));
   L.pc = off;
-  off = align256(off + precond_workspace_size(p, o));
+  off = align256(off + pc_bytes);
   L.total = off;
   return L;
 }
 
-}  // namespace cev
-
-using namespace cev;
-
-extern "C" {
-
-void cev_solve_opts_default(cev_solve_opts* o) {
-  if (!o) return;
-  o->tol = 1e-6;
-  o->inner_rtol = 1e-4;
-  o->max_iters = 20000;
-  o->restart = 30;
-  o->precond = CEV_PRECOND_NONE;
-  o->transpose = 0;
-  o->use_x0 = 0;
-  o->reorth = 0;
-  o->max_stall = 20;
-  o->mg_levels = 0;
-  o->mg_shift = 0.5;
-  o->learned = nullptr;
+static KrylovProblem stencil_problem(const cev_fdfd_plan_s* p) {
+  KrylovProblem P;
+  P.B = p->batch;
+  P.n = p->n();
+  dim3 g, bl;
+  int rows;
+  launch_geometry(p->nx, p->ny, p->batch, g, bl, rows);
+  P.res_blocks = (size_t)g.x * g.y;
+  P.extra_bytes = sizeof(float) * p->n() * p->batch;  // float copy of eps
+  return P;
 }
 
-size_t cev_fdfd_solve_workspace_size(cev_fdfd_plan p, const cev_solve_opts* opts) {
-  if (!p || !opts || opts->restart < 1 || opts->restart > 64) return 0;
-  return layout(p, *opts).total;
-}
-
-int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const void* bvec, void* xvec,
-                   const cev_solve_opts* opts, cev_solve_info* info, void* ws, size_t ws_bytes,
-                   cudaStream_t s) {
-  CEV_REQUIRE(p != nullptr, "plan is NULL");
-  CEV_REQUIRE(opts != nullptr, "opts is NULL");
-  CEV_REQUIRE(eps && bvec && xvec && info, "NULL argument");
-  const cev_solve_opts& o = *opts;
-  CEV_REQUIRE(o.restart >= 1 && o.restart <= 64, "restart must be in [1, 64], got %d", o.restart);
-  CEV_REQUIRE(o.tol > 0 && o.tol < 1, "tol must be in (0, 1)");
-  CEV_REQUIRE(o.max_iters >= 1, "max_iters must be >= 1");
-  CEV_REQUIRE(o.precond == CEV_PRECOND_NONE || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN ||
-                  o.precond == CEV_PRECOND_LEARNED,
-              "unknown preconditioner %d", o.precond);
-  const Layout L = layout(p, o);
-  CEV_REQUIRE(ws != nullptr && ws_bytes >= L.total,
-              "workspace too small: need %zu bytes, got %zu", L.total, ws_bytes);
-  CEV_REQUIRE(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
-
-  const size_t N = p->n();
-  const int B = p->batch, m = o.restart;
-  const int tr = o.transpose ? 1 : 0;
+// ------------------------------------------------------------ the driver
+int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opts& o,
+               const double2* bvec, double2* xvec, cev_solve_info* info, void* ws,
+               size_t ws_bytes, cudaStream_t s) {
+  const size_t N = P.n;
+  const int B = P.B, m = o.restart;
+  const bool flexible = o.precond != CEV_PRECOND_NONE;
+  const KLayout L = klayout(P, o, 0);
+  CEV_REQUIRE(ws_bytes >= L.pc, "workspace too small");
   char* w = (char*)ws;
   KCtx c;
   c.st = (KState*)(w + L.st);
@@ -627,66 +503,23 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
   c.tol = o.tol;
   c.inner_rtol = o.inner_rtol;
   c.max_iters = o.max_iters;
-  float* eps32 = (float*)(w + L.eps32);
   float2* V = (float2*)(w + L.V);
   float2* Z = (float2*)(w + L.Z);
-  const bool flexible = o.precond != CEV_PRECOND_NONE;
+  CEV_REQUIRE(!flexible || ops.precond, "preconditioner not available for this operator");
 
   CEV_CUDA(cudaMemsetAsync(c.counter, 0, sizeof(unsigned) * 2 * B, s));
   CEV_CUDA(cudaMemsetAsync(c.st, 0, sizeof(KState) * B, s));
-  const size_t ne = eps_shared ? N : N * B;
-  k_to_f32<<<std::min(ceil_div(ne, 256), 8u * sm_count()), 256, 0, s>>>(eps, eps32, ne);
   if (!o.use_x0)
-    k_zero_c128<<<std::min(ceil_div(N * B, 256), 8u * sm_count()), 256, 0, s>>>((double2*)xvec,
-                                                                               N * B);
-  CEV_CHECK_LAUNCH("solve init");
-
-  Precond pc;
-  int rc = precond_setup(pc, p, o, eps32, eps_shared, w + L.pc, s);
-  if (rc != CEV_OK) return rc;
-
-  dim3 sg, sb;
-  int rows;
-  launch_geometry(p->nx, p->ny, B, sg, sb, rows);
+    k_zero_c128<<<std::min(ceil_div(N * B, 256), 8u * sm_count()), 256, 0, s>>>(xvec, N * B);
   const dim3 rg(L.nblk, B, 1);
-
-  auto residual = [&](int first) -> int {
-    if (p->pol == POL_EZ) {
-      ResArgs<POL_EZ> a{p->nx, p->ny, rows, first, m, eps, eps_shared ? 0 : N,
-                        (const double2*)xvec, (const double2*)bvec, p->scale,
-                        p->cx64[tr], p->cy64[tr], p->k2_64, V, N, c};
-      k_residual<POL_EZ><<<sg, sb, 0, s>>>(a);
-    } else {
-      ResArgs<POL_HZ> a{p->nx, p->ny, rows, first, m, eps, eps_shared ? 0 : N,
-                        (const double2*)xvec, (const double2*)bvec, p->scale,
-                        p->cx64[tr], p->cy64[tr], p->k2_64, V, N, c};
-      k_residual<POL_HZ><<<sg, sb, 0, s>>>(a);
-    }
-    CEV_CHECK_LAUNCH("k_residual");
-    return CEV_OK;
-  };
-  auto matvec = [&](int j, const float2* in, size_t in_bs, int use_scale) -> int {
-    float2* out = V + (size_t)(j + 1) * B * N;
-    if (p->pol == POL_EZ) {
-      MvArgs<POL_EZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, in_bs, use_scale,
-                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
-      k_arnoldi_mv<POL_EZ><<<sg, sb, 0, s>>>(a);
-    } else {
-      MvArgs<POL_HZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, in_bs, use_scale,
-                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
-      k_arnoldi_mv<POL_HZ><<<sg, sb, 0, s>>>(a);
-    }
-    CEV_CHECK_LAUNCH("k_arnoldi_mv");
-    return CEV_OK;
-  };
+  k_bnorm<<<rg, RED_THREADS, 0, s>>>(bvec, ops.bscale, N, c);
+  CEV_CHECK_LAUNCH("k_bnorm");
+  int rc = ops.residual(c, V, s);
+  if (rc != CEV_OK) return rc;
 
   std::vector<KState> hst(B);
   std::vector<double> best(B, INFINITY);
   std::vector<int> stall(B, 0), status(B, CEV_NOT_CONVERGED), cycles(B, 0);
-  k_bnorm<<<rg, RED_THREADS, 0, s>>>((const double2*)bvec, p->scale, N, c);
-  CEV_CHECK_LAUNCH("k_bnorm");
-  if ((rc = residual(0)) != CEV_OK) return rc;
-  int total_iters = 0;
   for (int cyc = 0;; ++cyc) {
     CEV_CUDA(cudaMemcpyAsync(hst.data(), c.st, sizeof(KState) * B, cudaMemcpyDeviceToHost, s));
     CEV_CUDA(cudaStreamSynchronize(s));
@@ -717,17 +550,18 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
         any = true;
       }
     }
-    if (changed) CEV_CUDA(cudaMemcpyAsync(c.st, hst.data(), sizeof(KState) * B,
-                                          cudaMemcpyHostToDevice, s));
+    if (changed)
+      CEV_CUDA(cudaMemcpyAsync(c.st, hst.data(), sizeof(KState) * B, cudaMemcpyHostToDevice, s));
     if (!any) break;
     for (int j = 0; j < m; ++j) {
       const float2* vin = V + (size_t)j * B * N;
+      float2* vout = V + (size_t)(j + 1) * B * N;
       if (flexible) {
         float2* zj = Z + (size_t)j * B * N;
-        if ((rc = precond_apply(pc, c, j, m, vin, zj, s)) != CEV_OK) return rc;
-        if ((rc = matvec(j, zj, N, 0)) != CEV_OK) return rc;
+        if ((rc = ops.precond(c, j, vin, zj, s)) != CEV_OK) return rc;
+        if ((rc = ops.matvec(c, j, zj, 0, vout, s)) != CEV_OK) return rc;
       } else {
-        if ((rc = matvec(j, vin, N, 1)) != CEV_OK) return rc;
+        if ((rc = ops.matvec(c, j, vin, 1, vout, s)) != CEV_OK) return rc;
       }
       for (int pass = 0; pass < (o.reorth ? 2 : 1); ++pass) {
         const bool final_pass = pass == (o.reorth ? 1 : 0);
@@ -738,12 +572,11 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
       }
       CEV_CHECK_LAUNCH("arnoldi step");
     }
-    total_iters += m;
     k_trisolve<<<B, 64, 0, s>>>(c, B, m);
-    XupArgs xa{N, B, m, flexible ? 1 : 0, V, Z, (double2*)xvec, 1.0, c};
+    XupArgs xa{N, B, m, flexible ? 1 : 0, V, Z, xvec, 1.0, c};
     k_xupdate<<<rg, RED_THREADS, 0, s>>>(xa);
     CEV_CHECK_LAUNCH("cycle finish");
-    if ((rc = residual(0)) != CEV_OK) return rc;
+    if ((rc = ops.residual(c, V, s)) != CEV_OK) return rc;
   }
   int worst = CEV_OK;
   for (int b = 0; b < B; ++b) {
@@ -751,12 +584,116 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
     info[b].iterations = hst[b].iters;
     info[b].cycles = cycles[b];
     info[b].reserved = 0;
-    info[b].bnorm = hst[b].bnorm / p->scale;
+    info[b].bnorm = hst[b].bnorm / ops.bscale;
     info[b].residual = hst[b].bnorm > 0 ? hst[b].beta / hst[b].bnorm : 0.0;
     if (status[b] < 0) worst = std::min(worst, status[b]);
     else if (worst >= 0) worst = std::max(worst, status[b]);
   }
   return worst;
+}
+
+int validate_opts(const cev_solve_opts& o) {
+  CEV_REQUIRE(o.restart >= 1 && o.restart <= 64, "restart must be in [1, 64], got %d", o.restart);
+  CEV_REQUIRE(o.tol > 0 && o.tol < 1, "tol must be in (0, 1)");
+  CEV_REQUIRE(o.max_iters >= 1, "max_iters must be >= 1");
+  CEV_REQUIRE(o.precond == CEV_PRECOND_NONE || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN ||
+                  o.precond == CEV_PRECOND_LEARNED,
+              "unknown preconditioner %d", o.precond);
+  return CEV_OK;
+}
+
+}  // namespace cev
+
+using namespace cev;
+
+extern "C" {
+
+void cev_solve_opts_default(cev_solve_opts* o) {
+  if (!o) return;
+  o->tol = 1e-6;
+  o->inner_rtol = 1e-4;
+  o->max_iters = 20000;
+  o->restart = 30;
+  o->precond = CEV_PRECOND_NONE;
+  o->transpose = 0;
+  o->use_x0 = 0;
+  o->reorth = 0;
+  o->max_stall = 20;
+  o->mg_levels = 0;
+  o->mg_shift = 0.5;
+  o->learned = nullptr;
+}
+
+size_t cev_fdfd_solve_workspace_size(cev_fdfd_plan p, const cev_solve_opts* opts) {
+  if (!p || !opts || opts->restart < 1 || opts->restart > 64) return 0;
+  return klayout(stencil_problem(p), *opts, precond_workspace_size(p, *opts)).total;
+}
+
+int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const void* bvec, void* xvec,
+                   const cev_solve_opts* opts, cev_solve_info* info, void* ws, size_t ws_bytes,
+                   cudaStream_t s) {
+  CEV_REQUIRE(p != nullptr, "plan is NULL");
+  CEV_REQUIRE(opts != nullptr, "opts is NULL");
+  CEV_REQUIRE(eps && bvec && xvec && info, "NULL argument");
+  const cev_solve_opts& o = *opts;
+  int rc = validate_opts(o);
+  if (rc != CEV_OK) return rc;
+  const KrylovProblem P = stencil_problem(p);
+  const KLayout L = klayout(P, o, precond_workspace_size(p, o));
+  CEV_REQUIRE(ws != nullptr && ws_bytes >= L.total,
+              "workspace too small: need %zu bytes, got %zu", L.total, ws_bytes);
+  CEV_REQUIRE(((uintptr_t)ws & 255) == 0, "workspace must be 256-byte aligned");
+  const size_t N = p->n();
+  const int B = p->batch, m = o.restart;
+  const int tr = o.transpose ? 1 : 0;
+  float* eps32 = (float*)((char*)ws + L.extra);
+  const size_t ne = eps_shared ? N : N * B;
+  k_to_f32<<<std::min(ceil_div(ne, 256), 8u * sm_count()), 256, 0, s>>>(eps, eps32, ne);
+  CEV_CHECK_LAUNCH("k_to_f32");
+  dim3 sg, sb;
+  int rows;
+  launch_geometry(p->nx, p->ny, B, sg, sb, rows);
+
+  KrylovOps ops;
+  ops.bscale = p->scale;
+  ops.residual = [&](const KCtx& c, float2* V0, cudaStream_t st) -> int {
+    if (p->pol == POL_EZ) {
+      ResArgs<POL_EZ> a{p->nx, p->ny, rows, 0, m, eps, eps_shared ? 0 : N, (const double2*)xvec,
+                        (const double2*)bvec, p->scale, p->cx64[tr], p->cy64[tr], p->k2_64, V0, N,
+                        c};
+      k_residual<POL_EZ><<<sg, sb, 0, st>>>(a);
+    } else {
+      ResArgs<POL_HZ> a{p->nx, p->ny, rows, 0, m, eps, eps_shared ? 0 : N, (const double2*)xvec,
+                        (const double2*)bvec, p->scale, p->cx64[tr], p->cy64[tr], p->k2_64, V0, N,
+                        c};
+      k_residual<POL_HZ><<<sg, sb, 0, st>>>(a);
+    }
+    CEV_CHECK_LAUNCH("k_residual");
+    return CEV_OK;
+  };
+  ops.matvec = [&](const KCtx& c, int j, const float2* in, int use_scale, float2* out,
+                   cudaStream_t st) -> int {
+    if (p->pol == POL_EZ) {
+      MvArgs<POL_EZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, N, use_scale,
+                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
+      k_arnoldi_mv<POL_EZ><<<sg, sb, 0, st>>>(a);
+    } else {
+      MvArgs<POL_HZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, N, use_scale,
+                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
+      k_arnoldi_mv<POL_HZ><<<sg, sb, 0, st>>>(a);
+    }
+    CEV_CHECK_LAUNCH("k_arnoldi_mv");
+    return CEV_OK;
+  };
+  Precond pc;
+  if (o.precond != CEV_PRECOND_NONE) {
+    rc = precond_setup(pc, p, o, eps32, eps_shared, (char*)ws + L.pc, s);
+    if (rc != CEV_OK) return rc;
+    ops.precond = [&](const KCtx& c, int j, const float2* v, float2* z, cudaStream_t st) {
+      return precond_apply(pc, c, j, m, v, z, st);
+    };
+  }
+  return krylov_run(P, ops, o, (const double2*)bvec, (double2*)xvec, info, ws, ws_bytes, s);
 }
 
 }  // extern "C"

@@ -1,6 +1,8 @@
 // Krylov solver state shared by the solver and the preconditioners.
 #pragma once
 
+#include <functional>
+
 #include "fdfd_plan.hpp"
 
 namespace cev {
@@ -36,6 +38,40 @@ struct KCtx {
   double tol, inner_rtol;
   int max_iters;
 };
+
+// ------------------------------------------------------- generic driver
+// A Krylov problem: B independent systems of n unknowns each, stored
+// [B][n] (complex128 x and b in the caller's units).
+struct KrylovProblem {
+  int B = 1;
+  size_t n = 0;
+  size_t res_blocks = 1;   // most blocks a residual kernel uses per problem
+  size_t extra_bytes = 0;  // operator scratch at the start of the workspace
+};
+
+struct KLayout {
+  size_t extra, V, Z, partial, counter, st, H, cs, sn, gam, sc, y, hpass, pc, total;
+  size_t part_stride;
+  int nblk;
+};
+KLayout klayout(const KrylovProblem& P, const cev_solve_opts& o, size_t pc_bytes);
+
+// Operator hooks.  residual(): launch r = b' - A' x in FP64 for every problem,
+// write r / KState.rscale (complex64) into V_0 and finish the reduction with
+// residual_finish.  matvec(j, in, use_scale, out): out = A' (s in) with
+// s = sc[b][j] when use_scale.  b' = bscale * b is the system the cycle sees.
+struct KrylovOps {
+  std::function<int(const KCtx&, float2* V0, cudaStream_t)> residual;
+  std::function<int(const KCtx&, int j, const float2* in, int use_scale, float2* out,
+                    cudaStream_t)> matvec;
+  std::function<int(const KCtx&, int j, const float2* v, float2* z, cudaStream_t)> precond;
+  double bscale = 1.0;
+};
+
+int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opts& o,
+               const double2* b, double2* x, cev_solve_info* info, void* ws, size_t ws_bytes,
+               cudaStream_t s);
+int validate_opts(const cev_solve_opts& o);
 
 // Right preconditioner used by flexible GMRES: z = M^{-1} (sc_j v_j).
 struct Precond {

@@ -183,6 +183,41 @@ CEV_API int cev_fdfd_fields_jvp(cev_fdfd_plan plan, const double* eps, int eps_s
                                 const double* deps, const void* fz, void* df1, void* df2,
                                 cudaStream_t stream);
 
+/*
+ * Multi-frequency (time-modulated) Ez FDFD, ceviche/fdfd.py:247-359
+ * (fdfd_mf_ez).  The plan holds M = 2*nsb+1 sidebands W_m = omega + m*omega_mod
+ * (m = -nsb..nsb) sharing the centre-frequency PML tables; fields and sources
+ * are complex128 [M][nx][ny].  The modulation of harmonic k (k < nfreq) is
+ * given as c_k = delta_k * exp(1j*phi_k), complex128 [nfreq][nx][ny]:
+ *   A_mm = -(1/mu0)(Dxf Dxb + Dyf Dyb) - eps0 W_m^2 eps,
+ *   A_m,m+k+1 = -eps0/2 W_m^2 c_k,   A_m,m-k-1 = -eps0/2 W_m^2 conj(c_k).
+ * cev_fdfd_fields / cev_fdfd_fields_adjoint apply per sideband with W_m
+ * (fdfd.py:339-355).  Destroy with cev_fdfd_plan_destroy.
+ */
+CEV_API int cev_fdfd_mf_plan_create(cev_fdfd_plan* plan, int nx, int ny, double dL, double omega,
+                                    double omega_mod, int nsb, int npml_x, int npml_y,
+                                    double bloch_x, double bloch_y);
+/* y = A x or A^T x of the coupled system, complex128, SI units. */
+CEV_API int cev_fdfd_mf_apply(cev_fdfd_plan plan, const double* eps, int nfreq,
+                              const void* coupling, const void* x, void* y, int transpose,
+                              cudaStream_t stream);
+CEV_API size_t cev_fdfd_mf_solve_workspace_size(cev_fdfd_plan plan, int nfreq,
+                                                const cev_solve_opts* opts);
+/* Solves the coupled system (one Krylov problem of M*nx*ny unknowns); info: 1 record.
+ * Replaces sp_solve of fdfd_mf_ez._solve_fn (fdfd.py:328-337). */
+CEV_API int cev_fdfd_mf_solve(cev_fdfd_plan plan, const double* eps, int nfreq,
+                              const void* coupling, const void* b, void* x,
+                              const cev_solve_opts* opts, cev_solve_info* info, void* workspace,
+                              size_t workspace_bytes, cudaStream_t stream);
+/*
+ * Gradients through A given x and mu = A^{-T} conj(g): geps (double [nx][ny])
+ * += dL/d eps; gcoupling (complex128 [nfreq][nx][ny], may be NULL) += dL/dc_k
+ * in the PyTorch convention.  Restates the sp_solve entries VJP
+ * (ceviche/primitives.py:121-128) chained through fdfd.py:289-326.
+ */
+CEV_API int cev_fdfd_mf_grad(cev_fdfd_plan plan, int nfreq, const void* x, const void* mu,
+                             double* geps, void* gcoupling, cudaStream_t stream);
+
 /* ============================== FDTD ==================================== */
 
 typedef struct cev_fdtd_plan_s* cev_fdtd_plan;
