@@ -120,3 +120,45 @@ class fdfd_hz(fdfd):
     (ceviche/fdfd.py:194-244).  solve(Mz) -> (Ex, Ey, Hz)."""
 
     pol = "hz"
+
+
+class fdfd_mf_ez(fdfd):
+    """Multi-frequency (time-modulated) Ez FDFD, ceviche/fdfd.py:247-359.
+
+    fdfd_mf_ez(omega, dL, eps_r, omega_mod, delta, phi, Nsb, npml,
+    bloch_phases=None); delta, phi: (Nfreq, Nx, Ny) modulation depth and
+    phase of each harmonic.  solve(source) with source (2*Nsb+1, Nx, Ny)
+    returns (Hx, Hy, Ez), each (2*Nsb+1, Nx, Ny); differentiable in eps_r,
+    delta, phi and the source when those are torch tensors.
+    """
+
+    pol = "ez"
+
+    def __init__(self, omega, dL, eps_r, omega_mod, delta, phi, Nsb, npml, bloch_phases=None,
+                 **solver_opts):
+        super().__init__(omega, dL, eps_r, npml, bloch_phases=bloch_phases, **solver_opts)
+        self.omega_mod = omega_mod
+        self.delta = delta
+        self.phi = phi
+        self.Nsb = Nsb
+
+    def _vec_to_grid(self, vec):
+        return vec.reshape((2 * self.Nsb + 1,) + tuple(self.shape))
+
+    def solve(self, source_z):
+        tens = [torch.is_tensor(a) for a in (self.eps_r, self.delta, self.phi, source_z)]
+        numpy_out = not any(tens)
+        eps = _to_tensor(self.eps_r, torch.float64)
+        delta = _to_tensor(self.delta, torch.float64)
+        phi = _to_tensor(self.phi, torch.float64)
+        cpl = delta * torch.exp(1j * phi)
+        src = source_z if torch.is_tensor(source_z) else np.asarray(source_z)
+        cplx = (torch.is_tensor(src) and src.is_complex()) or \
+            (not torch.is_tensor(src) and np.iscomplexobj(src))
+        src = _to_tensor(src, torch.complex128 if cplx else torch.float64)
+        plan = prim.get_mf_plan(self.shape, self.dL, self.omega, self.omega_mod, self.Nsb,
+                                self.npml, (self.bloch_x, self.bloch_y))
+        out = prim.FDFDMFSolve.apply(eps, cpl, src, plan, self.solver_opts)
+        if numpy_out:
+            return tuple(f.detach().cpu().numpy() for f in out)
+        return out

@@ -316,3 +316,144 @@ class FDFDSolve(torch.autograd.Function):
         if deps is not None:
             fields_jvp(plan, eps, deps, x, df1, df2)
         return df1, df2, dx
+
+
+# ---------------------------------------------------- multi-frequency (mf) Ez
+class MFPlan:
+    """Owns a multi-frequency Ez plan: M = 2*Nsb+1 sidebands W_m sharing the
+    centre-frequency PML tables (ceviche/fdfd.py:247-359)."""
+
+    pol_name = "ez"
+
+    def __init__(self, shape, dL, omega, omega_mod, nsb, npml, bloch=(0.0, 0.0)):
+        _require_cuda()
+        lib = _lib.load()
+        self.nx, self.ny = int(shape[0]), int(shape[1])
+        self.nsb = int(nsb)
+        self.batch = 2 * self.nsb + 1
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        h = C.c_void_p()
+        check(lib.cev_fdfd_mf_plan_create(C.byref(h), self.nx, self.ny, float(dL), float(omega),
+                                          float(omega_mod), self.nsb, int(npml[0]), int(npml[1]),
+                                          float(bloch[0]), float(bloch[1])), "mf_plan_create")
+        self.handle = h
+        self.scale = lib.cev_fdfd_plan_scale(h)
+        W = omega + np.arange(-self.nsb, self.nsb + 1) * omega_mod
+        self.omega_t = torch.tensor(W, dtype=torch.float64, device=self.device)
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.cev_fdfd_plan_destroy(h)
+            self.handle = None
+
+    @property
+    def shape(self):
+        return (self.nx, self.ny)
+
+
+_mf_cache = {}
+
+
+def get_mf_plan(shape, dL, omega, omega_mod, nsb, npml, bloch=(0.0, 0.0)):
+    key = (int(shape[0]), int(shape[1]), float(dL), float(omega), float(omega_mod), int(nsb),
+           int(npml[0]), int(npml[1]), float(bloch[0]), float(bloch[1]),
+           torch.cuda.current_device())
+    p = _mf_cache.get(key)
+    if p is None:
+        if len(_mf_cache) > 16:
+            _mf_cache.clear()
+        p = _mf_cache[key] = MFPlan(shape, dL, omega, omega_mod, nsb, npml, bloch)
+    return p
+
+
+def _cpl_arg(plan, cpl):
+    if cpl is None or cpl.numel() == 0:
+        return torch.zeros((0, plan.nx, plan.ny), dtype=torch.complex128, device=plan.device), 0
+    c = cpl.to(device=plan.device, dtype=torch.complex128).reshape(-1, plan.nx, plan.ny)
+    c = c[: 2 * plan.nsb].contiguous()  # harmonics k >= 2*Nsb couple no sideband pair
+    return c, int(c.shape[0])
+
+
+def mf_apply(plan, eps, cpl, x, transpose=False):
+    lib = _lib.load()
+    e = eps.to(device=plan.device, dtype=torch.float64).reshape(plan.nx, plan.ny).contiguous()
+    c, nf = _cpl_arg(plan, cpl)
+    xt = _field_arg(plan, x, torch.complex128)
+    y = torch.empty_like(xt)
+    check(lib.cev_fdfd_mf_apply(plan.handle, ptr(e), nf, ptr(c), ptr(xt), ptr(y),
+                                int(bool(transpose)), stream_ptr()), "mf_apply")
+    return y
+
+
+def mf_solve(plan, eps, cpl, b, transpose=False, strict=False, **opts):
+    lib = _lib.load()
+    e = eps.to(device=plan.device, dtype=torch.float64).reshape(plan.nx, plan.ny).contiguous()
+    c, nf = _cpl_arg(plan, cpl)
+    bt = _field_arg(plan, b, torch.complex128)
+    s = make_opts(transpose=transpose, **opts)
+    x = torch.empty_like(bt)
+    nbytes = lib.cev_fdfd_mf_solve_workspace_size(plan.handle, nf, C.byref(s))
+    if nbytes == 0:
+        raise ValueError("invalid solver options")
+    ws, wptr = _workspace(nbytes, plan.device)
+    info = (_lib.SolveInfo * 1)()
+    rc = lib.cev_fdfd_mf_solve(plan.handle, ptr(e), nf, ptr(c), ptr(bt), ptr(x), C.byref(s), info,
+                               C.c_void_p(wptr), nbytes, stream_ptr())
+    check(rc, "mf_solve")
+    del ws
+    r = dict(status=_lib.STATUS_NAMES.get(info[0].status, info[0].status), code=info[0].status,
+             iterations=info[0].iterations, cycles=info[0].cycles, residual=info[0].residual)
+    if rc > 0:
+        msg = f"multi-frequency FDFD solve did not reach tol={s.tol:g}: {r}"
+        if strict:
+            raise _lib.CevError(msg)
+        warnings.warn(msg, SolverWarning, stacklevel=2)
+    return x, r
+
+
+class FDFDMFSolve(torch.autograd.Function):
+    """(eps, c, src) -> (Hx, Hy, Ez) of fdfd_mf_ez.solve with b_m = 1j W_m src_m
+    (ceviche/fdfd.py:328-337); c_k = delta_k exp(1j phi_k).  Backward: the
+    transposed coupled solve plus cev_fdfd_mf_grad."""
+
+    @staticmethod
+    def forward(ctx, eps, cpl, src, plan, opts):
+        W = plan.omega_t.view(-1, 1, 1)
+        b = 1j * W * _field_arg(plan, src, torch.complex128)
+        x, info = mf_solve(plan, eps, cpl, b, **opts)
+        f1, f2 = fields(plan, eps.reshape(plan.nx, plan.ny), x)
+        ctx.plan, ctx.opts = plan, opts
+        ctx.src_real = not src.is_complex()
+        ctx.save_for_backward(eps, cpl, x)
+        ctx.info = info
+        return f1, f2, x
+
+    @staticmethod
+    def backward(ctx, g1, g2, gz):
+        plan = ctx.plan
+        eps, cpl, x = ctx.saved_tensors
+        lib = _lib.load()
+        e = eps.reshape(plan.nx, plan.ny)
+        zeros = lambda: torch.zeros_like(x)
+        g1 = zeros() if g1 is None else g1.to(torch.complex128).contiguous()
+        g2 = zeros() if g2 is None else g2.to(torch.complex128).contiguous()
+        gx = zeros() if gz is None else gz.to(torch.complex128).contiguous().clone()
+        fields_adjoint(plan, e, x, g1, g2, gx, None)
+        mu, _ = mf_solve(plan, eps, cpl, gx.conj().resolve_conj(), transpose=True, **ctx.opts)
+        c, nf = _cpl_arg(plan, cpl)
+        geps = torch.zeros((plan.nx, plan.ny), dtype=torch.float64, device=plan.device)
+        gcpl = torch.zeros_like(c)
+        check(lib.cev_fdfd_mf_grad(plan.handle, nf, ptr(x), ptr(mu), ptr(geps), ptr(gcpl),
+                                   stream_ptr()), "mf_grad")
+        g_eps = geps.reshape(eps.shape) if ctx.needs_input_grad[0] else None
+        g_cpl = None
+        if ctx.needs_input_grad[1]:
+            g_cpl = torch.zeros_like(cpl, dtype=torch.complex128).reshape(-1, plan.nx, plan.ny)
+            g_cpl[:nf] = gcpl
+            g_cpl = g_cpl.reshape(cpl.shape)
+        g_src = None
+        if ctx.needs_input_grad[2]:
+            gs = -1j * plan.omega_t.view(-1, 1, 1) * mu.conj()
+            g_src = gs.real if ctx.src_real else gs
+        return g_eps, g_cpl, g_src, None, None

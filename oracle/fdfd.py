@@ -221,3 +221,50 @@ def grad_eps_hz(omega, dL, eps, npml, Mz, g_ex, g_ey, g_hz, source_times_eps=Fal
     if source_times_eps:
         grad = grad + np.real(-adj * 1j * omega * Mz.ravel()).reshape(shape)
     return grad
+
+
+# ------------------------------------------------- multi-frequency (fdfd_mf_ez)
+def make_A_mf_ez(omega, dL, eps, npml, omega_mod, delta, phi, Nsb, bloch=(0.0, 0.0)):
+    """Coupled sideband system of ceviche/fdfd.py:289-326: block-diagonal
+    Ez operators at the centre-frequency derivatives with -eps0 W_m^2 eps on the
+    diagonal, plus -eps0/2 W_m^2 delta_k exp(+-1j phi_k) coupling to sidebands
+    m +- (k+1)."""
+    M = 2 * Nsb + 1
+    N = eps.size
+    W = omega + np.arange(-Nsb, Nsb + 1) * omega_mod
+    Dxf, Dxb, Dyf, Dyb = derivative_matrices(omega, eps.shape, npml, dL, *bloch)
+    C = -1 / MU_0 * Dxf.dot(Dxb) - 1 / MU_0 * Dyf.dot(Dyb)
+    A = sp.kron(sp.eye(M), C) + sp.diags(-EPSILON_0 * np.kron(W ** 2, eps.ravel()))
+    A = A.tolil()
+    nfreq = delta.shape[0]
+    dmat = delta.reshape(nfreq, N)
+    pmat = phi.reshape(nfreq, N)
+    A = A.tocsr()
+    blocks = []
+    for k in range(nfreq):
+        mod_p = -0.5 * EPSILON_0 * dmat[k] * np.exp(1j * pmat[k])
+        mod_m = -0.5 * EPSILON_0 * dmat[k] * np.exp(-1j * pmat[k])
+        ent_p = np.kron(W[:-k - 1] ** 2, mod_p)
+        rows_p = np.arange((M - k - 1) * N)
+        blocks.append(sp.coo_matrix((ent_p, (rows_p, rows_p + (k + 1) * N)), shape=(M * N, M * N)))
+        ent_m = np.kron(W[k + 1:] ** 2, mod_m)
+        rows_m = np.arange((k + 1) * N, M * N)
+        blocks.append(sp.coo_matrix((ent_m, (rows_m, rows_m - (k + 1) * N)), shape=(M * N, M * N)))
+    for blk in blocks:
+        A = A + blk
+    return A.tocsr()
+
+
+def solve_mf_ez(omega, dL, eps, npml, omega_mod, delta, phi, Nsb, Jz, bloch=(0.0, 0.0)):
+    """(Hx, Hy, Ez), each (M, Nx, Ny): fdfd_mf_ez.solve (fdfd.py:262-283, 328-359)."""
+    M = 2 * Nsb + 1
+    shape = eps.shape
+    W = omega + np.arange(-Nsb, Nsb + 1) * omega_mod
+    A = make_A_mf_ez(omega, dL, eps, npml, omega_mod, delta, phi, Nsb, bloch)
+    b = 1j * (W[:, None] * Jz.reshape(M, -1)).ravel()
+    ez = spsolve(A, b).reshape(M, -1)
+    _, Dxb, _, Dyb = derivative_matrices(omega, shape, npml, dL, *bloch)
+    hx = np.stack([-1 / 1j / MU_0 / W[m] * Dyb.dot(ez[m]) for m in range(M)])
+    hy = np.stack([1 / 1j / MU_0 / W[m] * Dxb.dot(ez[m]) for m in range(M)])
+    r = lambda a: a.reshape((M,) + shape)
+    return r(hx), r(hy), r(ez)

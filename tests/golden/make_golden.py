@@ -12,6 +12,9 @@ Fixtures (all small, seeded):
     fdtd_fields.npz     fdtd.forward fields after TM and TE runs (fdtd.py:74-144)
     grad_fd.npz         central finite differences of reference objectives
                         (gradient pins for the FDFD and FDTD adjoints)
+    fdfd_mf.npz         fdfd_mf_ez system products and solve outputs
+                        (fdfd.py:247-359), plus central differences of a
+                        reference objective w.r.t. eps, delta and phi
 """
 import os
 import sys
@@ -179,7 +182,53 @@ def main(ref_root):
     out["fdtd_eps"], out["fdtd_prof"], out["fdtd_amps"] = eps0, prof[:, :, 0], amps
     out["fdtd_grad"], out["fdtd_S"] = g, np.array(S(eps0))
     np.savez_compressed(os.path.join(HERE, "grad_fd.npz"), **out)
+    make_mf(ceviche, utils, constants, np.random.default_rng(424242))
     print("fixtures written to", HERE)
+
+
+def make_mf(ceviche, utils, constants, rng):
+    out = {}
+    Nx, Ny, Nsb, nfreq = 22, 18, 2, 2
+    omega, omega_mod, dL, npml = 2 * np.pi * 200e12, 2 * np.pi * 4e12, 1e-6, [5, 4]
+    eps = rng.random((Nx, Ny)) + 1
+    delta = 0.3 * rng.random((nfreq, Nx, Ny))
+    phi = 2 * np.pi * rng.random((nfreq, Nx, Ny))
+    M = 2 * Nsb + 1
+    F = ceviche.fdfd_mf_ez(omega, dL, eps, omega_mod, delta, phi, Nsb, npml)
+    entries, indices = F._make_A(eps.ravel(), delta.reshape(nfreq, -1), phi.reshape(nfreq, -1))
+    A = utils.make_sparse(entries, indices, shape=(M * Nx * Ny, M * Nx * Ny))
+    x = rng.standard_normal(M * Nx * Ny) + 1j * rng.standard_normal(M * Nx * Ny)
+    src = np.zeros((M, Nx, Ny))
+    src[Nsb, Nx // 2, Ny // 2] = 1.0
+    src[Nsb + 1, 7, 5] = 0.4
+    out.update(eps=eps, delta=delta, phi=phi, x=x, Ax=A.dot(x), ATx=A.T.dot(x), src=src,
+               meta=np.array([Nsb, nfreq, omega, omega_mod, dL, npml[0], npml[1]]))
+    out["fields"] = np.stack(F.solve(src))
+
+    def J(e, d, p):
+        G = ceviche.fdfd_mf_ez(omega, dL, e, omega_mod, d, p, Nsb, npml)
+        hx, hy, ez = G.solve(src)
+        return np.sum(np.abs(ez) ** 2) + np.sum(np.abs(hx) ** 2) + 0.5 * np.sum(np.abs(hy) ** 2)
+
+    h = 1e-5
+    pix = rng.choice(Nx * Ny, size=8, replace=False)
+    ge, gd, gp = [], [], []
+    for q in pix:
+        e1, e2 = eps.copy(), eps.copy()
+        e1.flat[q] += h
+        e2.flat[q] -= h
+        ge.append((J(e1, delta, phi) - J(e2, delta, phi)) / (2 * h))
+        d1, d2 = delta.copy(), delta.copy()
+        d1[1].flat[q] += h
+        d2[1].flat[q] -= h
+        gd.append((J(eps, d1, phi) - J(eps, d2, phi)) / (2 * h))
+        p1, p2 = phi.copy(), phi.copy()
+        p1[0].flat[q] += h
+        p2[0].flat[q] -= h
+        gp.append((J(eps, delta, p1) - J(eps, delta, p2)) / (2 * h))
+    out.update(pix=pix, grad_eps=np.array(ge), grad_delta1=np.array(gd), grad_phi0=np.array(gp),
+               J=np.array(J(eps, delta, phi)))
+    np.savez_compressed(os.path.join(HERE, "fdfd_mf.npz"), **out)
 
 
 if __name__ == "__main__":

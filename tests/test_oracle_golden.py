@@ -90,3 +90,16 @@ def test_fdtd_adjoint_matches_reference_fd():
     eps, prof, amps = d["fdtd_eps"], d["fdtd_prof"], d["fdtd_amps"]
     grad = oft.adjoint_tm(eps, 5e-8, [2, 2, 0], prof, amps, np.ones_like(eps), np.ones(len(amps)))
     assert _rel(grad.ravel(), d["fdtd_grad"]) < 1e-6
+
+
+def test_mf_operator_and_fields_match_reference():
+    d = _load("fdfd_mf.npz")
+    Nsb, nfreq, omega, omega_mod, dL, px, py = d["meta"]
+    Nsb = int(Nsb)
+    npml = [int(px), int(py)]
+    A = ofd.make_A_mf_ez(omega, dL, d["eps"], npml, omega_mod, d["delta"], d["phi"], Nsb)
+    assert _rel(A.dot(d["x"]), d["Ax"]) < 1e-13
+    assert _rel(A.T.dot(d["x"]), d["ATx"]) < 1e-13
+    f = ofd.solve_mf_ez(omega, dL, d["eps"], npml, omega_mod, d["delta"], d["phi"], Nsb, d["src"])
+    for got, ref in zip(f, d["fields"]):
+        assert _rel(got, ref) < 1e-10
