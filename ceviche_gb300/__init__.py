@@ -10,4 +10,5 @@ __version__ = "0.1.3+gb300"
 from .fdfd import fdfd_ez, fdfd_hz, fdfd_mf_ez  # noqa: F401
 from .fdtd import fdtd, fdtd_probe_series  # noqa: F401
 from .jacobians import jacobian  # noqa: F401
+from .sparse import sp_mult, sp_solve  # noqa: F401
 from . import constants, primitives  # noqa: F401

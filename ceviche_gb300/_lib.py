@@ -75,6 +75,10 @@ SIGNATURES = {
     "cev_fdfd_mf_solve": (I, [P, P, I, P, P, P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), P, S,
                               P]),
     "cev_fdfd_mf_grad": (I, [P, I, P, P, P, P, P]),
+    "cev_csr_apply": (I, [I, I, P, P, P, P, P, P]),
+    "cev_csr_solve_workspace_size": (S, [I, I, C.POINTER(SolveOpts)]),
+    "cev_csr_solve": (I, [I, I, P, P, P, D, P, P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), P, S,
+                          P]),
     "cev_fdtd_plan_create": (I, [PP, I, I, D, I, I, I, P, P]),
     "cev_fdtd_plan_destroy": (I, [P]),
     "cev_fdtd_set_eps": (I, [P, P, P]),
@@ -133,4 +137,6 @@ def ptr(t):
     """Device pointer of a torch tensor (None -> NULL)."""
     if t is None:
         return None
+    if t.is_conj() or t.is_neg():
+        raise ValueError("lazily conjugated/negated tensor: call resolve_conj()/resolve_neg()")
     return C.c_void_p(t.data_ptr())

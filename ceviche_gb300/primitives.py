@@ -84,7 +84,7 @@ def get_plan(pol, shape, dL, omegas, npml, bloch=(0.0, 0.0)):
 
 def _eps_arg(plan, eps, dtype):
     """eps as a contiguous (1 or batch, nx, ny) device tensor; returns (eps, shared)."""
-    e = eps.to(device=plan.device, dtype=dtype).contiguous()
+    e = eps.to(device=plan.device, dtype=dtype).resolve_neg().contiguous()
     if e.dim() == 2:
         e = e.unsqueeze(0)
     if e.shape[-2:] != (plan.nx, plan.ny):
@@ -104,7 +104,7 @@ def _field_arg(plan, x, dtype):
         else:
             raise ValueError(f"field shape {tuple(t.shape)} does not match "
                              f"({plan.batch}, {plan.nx}, {plan.ny})")
-    return t.contiguous()
+    return t.resolve_conj().resolve_neg().contiguous()
 
 
 def apply(plan, eps, x, transpose=False, precision="c128", si_units=True):

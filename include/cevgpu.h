@@ -218,6 +218,27 @@ CEV_API int cev_fdfd_mf_solve(cev_fdfd_plan plan, const double* eps, int nfreq,
 CEV_API int cev_fdfd_mf_grad(cev_fdfd_plan plan, int nfreq, const void* x, const void* mu,
                              double* geps, void* gcoupling, cudaStream_t stream);
 
+/* ======================= generic sparse (CSR) ============================ */
+/*
+ * y = A x for a complex128 CSR matrix (n x n, nnz entries, int32 indices):
+ * sp_mult of ceviche/primitives.py:58-72 for entries/indices that are not a
+ * Yee stencil.  The caller builds CSR from COO with duplicates summed
+ * (ceviche/utils.py:13-25); A^T is applied by passing the transpose's CSR.
+ */
+CEV_API int cev_csr_apply(int n, int nnz, const int* row_ptr, const int* col, const void* val,
+                          const void* x, void* y, cudaStream_t stream);
+CEV_API size_t cev_csr_solve_workspace_size(int n, int nnz, const cev_solve_opts* opts);
+/*
+ * x = A^{-1} b (sp_solve, ceviche/primitives.py:103-119) with the same
+ * mixed-precision restarted GMRES as cev_fdfd_solve, on the scaled system
+ * (scale*A) x = scale*b; pass scale ~ 1/max|A_ij| so the complex64 cycle
+ * stays in range.  info: 1 record.
+ */
+CEV_API int cev_csr_solve(int n, int nnz, const int* row_ptr, const int* col, const void* val,
+                          double scale, const void* b, void* x, const cev_solve_opts* opts,
+                          cev_solve_info* info, void* workspace, size_t workspace_bytes,
+                          cudaStream_t stream);
+
 /* ============================== FDTD ==================================== */
 
 typedef struct cev_fdtd_plan_s* cev_fdtd_plan;
