@@ -239,6 +239,16 @@ CEV_API int cev_csr_solve(int n, int nnz, const int* row_ptr, const int* col, co
                           cev_solve_info* info, void* workspace, size_t workspace_bytes,
                           cudaStream_t stream);
 
+/* ---------------------------------------------------------------- probes
+ * Replaces the per-step host loop of ceviche.utils.measure_fields
+ * (ceviche/utils.py:316-332): out[t*out_stride + p] = sum_q weight[q] *
+ * field[t*field_stride + cell[q]] for q in probe_ptr[p] .. probe_ptr[p+1]-1,
+ * t = 0 .. nrows-1, accumulated in FP64 (deterministic).  field is float32
+ * (field_is_f64 = 0) or float64; probe_ptr has n_probe + 1 entries; nrows <= 65535. */
+CEV_API int cev_probe_measure(int n_probe, const int* probe_ptr, const int* cell, const double* weight,
+                              const void* field, int field_is_f64, int nrows, long long field_stride,
+                              double* out, long long out_stride, cudaStream_t stream);
+
 /* ============================== FDTD ==================================== */
 
 typedef struct cev_fdtd_plan_s* cev_fdtd_plan;

@@ -183,6 +183,20 @@ def run_tm(eps, dL, npml, src_profile, amps, record_every=None):
     return F, snaps
 
 
+def measure_fields(F, source, steps, probes, component="Ez"):
+    """ceviche/utils.py:316-332 on an FDTD2D: reset, then per step
+    F.forward(Jz=source(t)) and sum(field * probe) for each probe."""
+    F.reset()
+    if not isinstance(probes, list):
+        probes = [probes]
+    measured = np.zeros((steps, len(probes)))
+    for t in range(steps):
+        f = F.forward(Jz=source(t))
+        for k, p in enumerate(probes):
+            measured[t, k] = np.sum(f[component] * np.reshape(p, f[component].shape))
+    return measured
+
+
 def adjoint_tm(eps, dL, npml, src_profile, amps, probe, weights):
     """dL/d(eps) for L = sum_t weights[t] * sum(probe * Ez_t), with the TM
     recurrence of ``FDTD2D.forward`` (Jz = src_profile * amps[t], eps-independent).

@@ -15,6 +15,8 @@ Fixtures (all small, seeded):
     fdfd_mf.npz         fdfd_mf_ez system products and solve outputs
                         (fdfd.py:247-359), plus central differences of a
                         reference objective w.r.t. eps, delta and phi
+    measure.npz         utils.measure_fields time series (utils.py:316-332)
+                        of Ez and Hx at three probes
 """
 import os
 import sys
@@ -183,6 +185,7 @@ def main(ref_root):
     out["fdtd_grad"], out["fdtd_S"] = g, np.array(S(eps0))
     np.savez_compressed(os.path.join(HERE, "grad_fd.npz"), **out)
     make_mf(ceviche, utils, constants, np.random.default_rng(424242))
+    make_measure(ceviche, utils, np.random.default_rng(515151))
     print("fixtures written to", HERE)
 
 
@@ -229,6 +232,32 @@ def make_mf(ceviche, utils, constants, rng):
     out.update(pix=pix, grad_eps=np.array(ge), grad_delta1=np.array(gd), grad_phi0=np.array(gp),
                J=np.array(J(eps, delta, phi)))
     np.savez_compressed(os.path.join(HERE, "fdfd_mf.npz"), **out)
+
+
+def make_measure(ceviche, utils, rng):
+    """measure_fields on a 34x28 grid with rods, a pulsed line source and
+    three probes (a point, a weighted line, a random patch)."""
+    import contextlib
+    import io
+    Nx, Ny, steps = 34, 28, 160
+    eps = 1 + 3 * rng.random((Nx, Ny, 1))
+    prof = np.zeros((Nx, Ny, 1))
+    prof[10, 8:16, 0] = 1.0
+    t = np.arange(steps)
+    amps = np.exp(-((t - 40) / 12.0) ** 2) * np.cos(0.35 * t)
+    probes = [np.zeros((Nx, Ny, 1)) for _ in range(3)]
+    probes[0][20, 14, 0] = 1.0
+    probes[1][25, 4:24, 0] = np.linspace(-1, 2, 20)
+    probes[2][3:9, 18:26, 0] = rng.standard_normal((6, 8))
+    out = dict(eps=eps[:, :, 0], prof=prof[:, :, 0], amps=amps,
+               probes=np.stack([p[:, :, 0] for p in probes]), meta=np.array([5e-8, 6, 5]))
+    F = ceviche.fdtd(eps, dL=5e-8, npml=[6, 5, 0])
+    src = lambda k: prof * amps[k]  # noqa: E731
+    with contextlib.redirect_stdout(io.StringIO()):  # the reference prints progress
+        out["Ez"] = utils.measure_fields(F, src, steps, probes, component="Ez")
+        out["Hx"] = utils.measure_fields(F, src, steps, probes, component="Hx")
+        out["Ez_single"] = utils.measure_fields(F, src, steps, probes[1], component="Ez")
+    np.savez_compressed(os.path.join(HERE, "measure.npz"), **out)
 
 
 if __name__ == "__main__":

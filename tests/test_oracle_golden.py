@@ -103,3 +103,18 @@ def test_mf_operator_and_fields_match_reference():
     f = ofd.solve_mf_ez(omega, dL, d["eps"], npml, omega_mod, d["delta"], d["phi"], Nsb, d["src"])
     for got, ref in zip(f, d["fields"]):
         assert _rel(got, ref) < 1e-10
+
+
+def test_measure_fields_matches_reference():
+    """oracle.fdtd.measure_fields vs the reference's utils.measure_fields."""
+    d = np.load(os.path.join(GOLDEN, "measure.npz"))
+    dL, px, py = d["meta"]
+    F = oft.FDTD2D(d["eps"], dL, [int(px), int(py), 0])
+    src = lambda t: d["prof"] * d["amps"][t]  # noqa: E731
+    probes = list(d["probes"])
+    steps = len(d["amps"])
+    for comp in ("Ez", "Hx"):
+        m = oft.measure_fields(F, src, steps, probes, component=comp)
+        assert np.linalg.norm(m - d[comp]) <= 1e-12 * np.linalg.norm(d[comp]), comp
+    m = oft.measure_fields(F, src, steps, d["probes"][1], component="Ez")
+    assert np.linalg.norm(m - d["Ez_single"]) <= 1e-12 * np.linalg.norm(d["Ez_single"])
