@@ -80,6 +80,9 @@ SIGNATURES = {
     "cev_csr_solve": (I, [I, I, P, P, P, D, P, P, C.POINTER(SolveOpts), C.POINTER(SolveInfo), P, S,
                           P]),
     "cev_probe_measure": (I, [I, P, P, P, P, I, I, C.c_longlong, P, C.c_longlong, P]),
+    "cev_mode_workspace_size": (S, [I, I, I]),
+    "cev_mode_solve": (I, [I, I, P, D, D, I, I, D, I, P, P, P, P, P, S, P]),
+    "cev_dense_eig": (I, [I, P, P, P]),
     "cev_fdtd_plan_create": (I, [PP, I, I, D, I, I, I, P, P]),
     "cev_fdtd_plan_destroy": (I, [P]),
     "cev_fdtd_set_eps": (I, [P, P, P]),

@@ -249,6 +249,29 @@ CEV_API int cev_probe_measure(int n_probe, const int* probe_ptr, const int* cell
                               const void* field, int field_is_f64, int nrows, long long field_stride,
                               double* out, long long out_stride, cudaStream_t stream);
 
+/* ----------------------------------------------------------------- modes
+ * Replaces ceviche.modes.get_modes (ceviche/modes.py:10-45) and the
+ * shift-invert ARPACK call behind it (solver_eigs, modes.py:68-78): for each
+ * of `batch` cross sections eps[b][0..n-1] (double, device), the m eigenpairs
+ * of A = diag(eps) + Dxf Dxb / k0^2 (k0 = omega / C_0; the (n, 1)-grid SC-PML
+ * derivatives of derivatives.py with npml cells per side and a periodic wrap)
+ * nearest sigma = max(eps), nearest first.  Outputs (device): vals complex128
+ * [batch][m] (n_eff^2), vecs complex128 [batch][m][n] with unit 2-norm and
+ * the largest-magnitude entry real positive (the reference's phase is
+ * ARPACK's, arbitrary), iters / status int [batch] (0 converged to tol, 1 not
+ * converged after max_iters, 2 singular shift).  n >= 3, 1 <= m <= min(n, 24).
+ * Synchronises the stream before returning. */
+CEV_API size_t cev_mode_workspace_size(int batch, int n, int m);
+CEV_API int cev_mode_solve(int batch, int n, const double* eps, double omega, double dL, int npml, int m,
+                           double tol, int max_iters, void* vals, void* vecs, int* iters, int* status,
+                           void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
+/* Host-side eigen-decomposition of a small dense complex matrix (k <= 24;
+ * the Rayleigh-Ritz step of cev_mode_solve, exported for checking): h, w, v
+ * are interleaved complex128 host arrays, h and v row-major k x k, column j of
+ * v the unit eigenvector of w[j].  No CUDA call. */
+CEV_API int cev_dense_eig(int k, const double* h, double* w, double* v);
+
 /* ============================== FDTD ==================================== */
 
 typedef struct cev_fdtd_plan_s* cev_fdtd_plan;

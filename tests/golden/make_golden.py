@@ -17,6 +17,9 @@ Fixtures (all small, seeded):
                         reference objective w.r.t. eps, delta and phi
     measure.npz         utils.measure_fields time series (utils.py:316-332)
                         of Ez and Hx at three probes
+    modes.npz           modes.get_modes eigenvalues and eigenvectors
+                        (modes.py:10-45; ARPACK phase, compare up to phase)
+                        and an insert_mode source (modes.py:48-65)
 """
 import os
 import sys
@@ -186,6 +189,7 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, "grad_fd.npz"), **out)
     make_mf(ceviche, utils, constants, np.random.default_rng(424242))
     make_measure(ceviche, utils, np.random.default_rng(515151))
+    make_modes(ceviche, constants, np.random.default_rng(616161))
     print("fixtures written to", HERE)
 
 
@@ -258,6 +262,41 @@ def make_measure(ceviche, utils, rng):
         out["Hx"] = utils.measure_fields(F, src, steps, probes, component="Hx")
         out["Ez_single"] = utils.measure_fields(F, src, steps, probes[1], component="Ez")
     np.savez_compressed(os.path.join(HERE, "measure.npz"), **out)
+
+
+def mode_cases(rng):
+    """(eps_cross, lambda, dL, npml, m): slab guides, a coupled pair, PML."""
+    cases = []
+    e = np.ones(120)
+    e[50:70] = 12.25
+    e[30:36] = 4.0
+    cases.append((e, 1.55e-6, 50e-9, 0, 4))
+    cases.append((e, 1.55e-6, 50e-9, 10, 3))
+    e2 = np.ones(160)
+    e2[40:52] = 9.0
+    e2[100:112] = 9.0  # two identical guides: near-degenerate even/odd pair
+    cases.append((e2, 1.3e-6, 40e-9, 12, 4))
+    e3 = 1 + 2 * rng.random(64)
+    e3[20:40] += 8.0
+    cases.append((e3, 1.8e-6, 60e-9, 5, 2))
+    return cases
+
+
+def make_modes(ceviche, constants, rng):
+    from ceviche import modes
+    out = {}
+    for c, (e, lam, dL, npml, m) in enumerate(mode_cases(rng)):
+        omega = 2 * np.pi * constants.C_0 / lam
+        vals, vecs = modes.get_modes(e, omega, dL, npml, m=m, filtering=False)
+        out[f"eps{c}"], out[f"vals{c}"], out[f"vecs{c}"] = e, vals, vecs
+        out[f"meta{c}"] = np.array([omega, dL, npml, m])
+    # insert_mode on a 2D permittivity: m = 2 profile across a slice
+    epsr = np.ones((40, 90))
+    epsr[:, 38:50] = 12.25
+    omega = 2 * np.pi * constants.C_0 / 1.55e-6
+    out["ins_epsr"] = epsr
+    out["ins_src"] = modes.insert_mode(omega, 50e-9, 10, slice(5, 85), epsr, m=2)
+    np.savez_compressed(os.path.join(HERE, "modes.npz"), **out)
 
 
 if __name__ == "__main__":

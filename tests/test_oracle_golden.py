@@ -118,3 +118,35 @@ def test_measure_fields_matches_reference():
         assert np.linalg.norm(m - d[comp]) <= 1e-12 * np.linalg.norm(d[comp]), comp
     m = oft.measure_fields(F, src, steps, d["probes"][1], component="Ez")
     assert np.linalg.norm(m - d["Ez_single"]) <= 1e-12 * np.linalg.norm(d["Ez_single"])
+
+
+def _same_up_to_phase(a, b, clusters=()):
+    """Columns of a and b equal up to a unit phase; column groups listed in
+    clusters (near-degenerate eigenvalues) compared as subspaces."""
+    done = set()
+    for grp in clusters:
+        qa, qb = np.linalg.qr(a[:, grp])[0], np.linalg.qr(b[:, grp])[0]
+        s = np.linalg.svd(qa.conj().T @ qb, compute_uv=False)  # principal angle cosines
+        assert np.all(np.abs(s - 1) < 1e-8), s
+        done |= set(grp)
+    for j in range(a.shape[1]):
+        if j not in done:
+            assert abs(abs(np.vdot(a[:, j], b[:, j])) - 1) < 1e-10, j
+
+
+def test_modes_match_reference():
+    """oracle.modes.get_modes vs the reference's ARPACK get_modes."""
+    from oracle import modes as om
+    d = np.load(os.path.join(GOLDEN, "modes.npz"))
+    for c in range(4):
+        omega, dL, npml, m = d[f"meta{c}"]
+        vals, vecs = om.get_modes(d[f"eps{c}"], omega, dL, int(npml), int(m), filtering=False)
+        ref_v = d[f"vals{c}"]
+        clusters = [(0, 1)] if c == 2 else []  # even/odd pair split by 3e-11
+        assert np.max(np.abs(np.sort_complex(vals) - np.sort_complex(ref_v))) < 1e-9
+        _same_up_to_phase(vecs, d[f"vecs{c}"], clusters)
+    src = om.insert_mode(omega=2 * np.pi * om.C_0 / 1.55e-6, dx=50e-9, x=10, y=slice(5, 85),
+                         epsr=d["ins_epsr"], m=2)
+    ref = d["ins_src"]
+    assert abs(abs(np.vdot(src[10, 5:85], ref[10, 5:85])) - 1) < 1e-10
+    assert np.all(src[np.arange(40) != 10] == 0)
