@@ -18,7 +18,8 @@ struct KState {
   int iters;       // total Arnoldi iterations
   int nan;         // non-finite value seen
   int done;        // host decided the problem is finished
-  int pad[3];
+  int fault;       // a bounded device wait timed out (fused cycle)
+  int pad[2];
   double rscale;   // the complex64 copy of the residual is stored divided by this
 };
 
@@ -35,6 +36,8 @@ struct KCtx {
   double* sc;           // [B][m+1] 1/||v_k|| (basis stored unnormalised)
   double2* y;           // [B][m] least-squares solution
   double2* hpass;       // [B][m+1] projections of the current pass
+  double* fpart;        // fused cycle: per-block partials
+  unsigned* bar;        // fused cycle: grid barrier words (count, generation, fault)
   double tol, inner_rtol;
   int max_iters;
 };
@@ -50,7 +53,7 @@ struct KrylovProblem {
 };
 
 struct KLayout {
-  size_t extra, V, Z, partial, counter, st, H, cs, sn, gam, sc, y, hpass, pc, total;
+  size_t extra, V, Z, partial, counter, st, H, cs, sn, gam, sc, y, hpass, fpart, pc, total;
   size_t part_stride;
   int nblk;
 };
@@ -65,8 +68,29 @@ struct KrylovOps {
   std::function<int(const KCtx&, int j, const float2* in, int use_scale, float2* out,
                     cudaStream_t)> matvec;
   std::function<int(const KCtx&, int j, const float2* v, float2* z, cudaStream_t)> precond;
+  // Optional: the whole Arnoldi cycle of an unpreconditioned single problem
+  // in one launch (replaces the per-iteration matvec / dot / update launches).
+  std::function<int(const KCtx&, float2* V, cudaStream_t)> cycle;
   double bscale = 1.0;
 };
+
+// Fused single-problem stencil cycle (cycle.cu).
+struct CycArgs {
+  int nx, ny, rows, m, reorth, tiles_y, units;
+  size_t N;
+  const float* eps;
+  const Coef<float>* cx;
+  const Coef<float>* cy;
+  const float* k2;
+  float2* V;  // [m+1][N]
+  KCtx ctx;
+};
+int fused_max_blocks();
+size_t cycle_stage_bytes();
+// Blocks of the fused cycle for an nx x ny grid (0: not available) and its
+// work split; limit > 0 caps the blocks (each then loops over several units).
+int cycle_plan(int nx, int ny, int pol, int limit, int& rows, int& tiles_y, int& units);
+int cycle_launch(int pol, int blocks, const CycArgs& a, cudaStream_t s);
 
 int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opts& o,
                const double2* b, double2* x, cev_solve_info* info, void* ws, size_t ws_bytes,

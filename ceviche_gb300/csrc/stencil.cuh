@@ -39,12 +39,23 @@ __device__ __forceinline__ R hz_d(R a, R b) {
   return R(1) / (R(0.5) * (a + b) + R(1e-5));
 }
 
+// Loads of the stencil input: the read-only path (the input is not written
+// during the launch), or with CG = true through L2 only (ld.global.cg), for
+// kernels that read vectors other blocks wrote earlier in the same launch.
+template <bool CG, typename T>
+__device__ __forceinline__ T ldx(const T* p) {
+  if constexpr (CG)
+    return __ldcg(p);
+  else
+    return __ldg(p);
+}
+
 // Sliding-window row iterator over one column j for rows [i0, i1).
 // Calls ep(i, Au, u_c) for every row with Au the stencil (without output
 // scaling) and u_c the centre value.
-template <typename R, int POL, typename Epi>
+template <typename R, int POL, typename Epi, bool CG = false>
 __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, int i1,
-                                               const Cplx<R>* __restrict__ x,
+                                               const Cplx<R>* x,
                                                const R* __restrict__ eps,
                                                const Coef<R>* __restrict__ cx,
                                                const Coef<R>& cyj, R k2, Epi& ep) {
@@ -53,8 +64,8 @@ __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, in
   const int jp = (j == ny - 1) ? 0 : j + 1;
   const int jmm = (jm == 0) ? ny - 1 : jm - 1;
   const int im0 = (i0 == 0) ? nx - 1 : i0 - 1;
-  C u_m = x[(size_t)im0 * ny + j];
-  C u_c = x[(size_t)i0 * ny + j];
+  C u_m = ldx<CG>(x + (size_t)im0 * ny + j);
+  C u_c = ldx<CG>(x + (size_t)i0 * ny + j);
   // Hz: eps window along i (for d_yy) ; Ez: unused
   R e_m = R(0), dyy_m = R(0);
   if (POL == POL_HZ) {
@@ -66,9 +77,9 @@ __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, in
   for (int i = i0; i < i1; ++i) {
     const int ip = (i == nx - 1) ? 0 : i + 1;
     const size_t row = (size_t)i * ny;
-    const C u_p = x[(size_t)ip * ny + j];
-    const C u_l = x[row + jm];
-    const C u_r = x[row + jp];
+    const C u_p = ldx<CG>(x + (size_t)ip * ny + j);
+    const C u_l = ldx<CG>(x + row + jm);
+    const C u_r = ldx<CG>(x + row + jp);
     const Coef<R> c = cx[i];
     C acc;
     if (POL == POL_EZ) {

@@ -227,3 +227,37 @@ def test_solve_extreme_rhs_magnitudes(cev, pol, mag):
         A = A.T if tr else A
         assert info[0]["code"] == 0
         assert ofd.true_residual(A, x.cpu().numpy().ravel(), b.ravel()) < 1e-9
+
+
+@pytest.mark.parametrize("pol", ["ez", "hz"])
+@pytest.mark.parametrize("reorth", [0, 1])
+@pytest.mark.parametrize("shape,blocks", [((90, 77), None), ((61, 300), None), ((70, 40), "5")])
+def test_fused_cycle_matches_multikernel(cev, pol, reorth, shape, blocks, monkeypatch):
+    """The single-launch restart cycle (one problem) against the per-iteration
+    launch path: both reach the FP64 tolerance (1e-7), the iterates agree to
+    1e-5 relative and the iteration counts within 10%.  Shapes cover one and two
+    column tiles and (CEV_FUSED_BLOCKS=5) blocks looping over several units."""
+    from ceviche_gb300 import primitives as P
+    rng = np.random.default_rng(17)
+    Nx, Ny = shape
+    dL, npml = 40e-9, [8, 7]
+    om = 2 * np.pi * 3e8 / 1.5e-6
+    eps = torch.as_tensor(rng.uniform(1, 5, (Nx, Ny)))
+    b = torch.as_tensor(rng.standard_normal((Nx, Ny)) + 1j * rng.standard_normal((Nx, Ny)))
+    plan = P.get_plan(pol, (Nx, Ny), dL, [om], npml)
+    if blocks:
+        monkeypatch.setenv("CEV_FUSED_BLOCKS", blocks)
+    out = {}
+    for mode in ("fused", "multi"):
+        if mode == "multi":
+            monkeypatch.setenv("CEV_FUSED_CYCLE", "0")
+        for tr in (False, True):
+            x, info = P.solve(plan, eps, b, transpose=tr, tol=1e-7, reorth=reorth, strict=True)
+            A = ofd.make_A(pol, om, dL, eps.numpy(), npml)
+            A = A.T if tr else A
+            assert ofd.true_residual(A, x.cpu().numpy().ravel(), b.numpy().ravel()) < 1e-7
+            out[mode, tr] = (x.cpu().numpy(), info[0]["iterations"])
+    for tr in (False, True):
+        (xf, itf), (xm, itm) = out["fused", tr], out["multi", tr]
+        assert _rel(xf, xm) < 1e-5, (itf, itm)
+        assert abs(itf - itm) <= 0.1 * itm + 2, (itf, itm)
