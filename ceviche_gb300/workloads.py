@@ -31,13 +31,17 @@ def rods_eps(Nx, Ny, npml, n_rods, rng):
     """eps 1 plus n_rods circular rods (radius 4..12 cells, eps ~ U[2, 12.25])
     centred in the non-PML interior; later rods overwrite earlier ones."""
     eps = np.ones((Nx, Ny))
-    I, J = np.meshgrid(np.arange(Nx), np.arange(Ny), indexing="ij")
     for _ in range(n_rods):
         ci = rng.uniform(npml, Nx - npml)
         cj = rng.uniform(npml, Ny - npml)
         r = rng.integers(4, 13)
         e = rng.uniform(2.0, 12.25)
-        eps[(I - ci) ** 2 + (J - cj) ** 2 <= r * r] = e
+        # only the rod's bounding window can satisfy the disc test
+        i0, i1 = max(0, int(np.floor(ci - r))), min(Nx, int(np.ceil(ci + r)) + 1)
+        j0, j1 = max(0, int(np.floor(cj - r))), min(Ny, int(np.ceil(cj + r)) + 1)
+        I, J = np.meshgrid(np.arange(i0, i1), np.arange(j0, j1), indexing="ij")
+        win = eps[i0:i1, j0:j1]
+        win[(I - ci) ** 2 + (J - cj) ** 2 <= r * r] = e
     return eps
 
 
