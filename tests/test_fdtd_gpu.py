@@ -147,7 +147,7 @@ def test_adjoint_matches_oracle_with_pml_and_probe(cev):
     assert _rel(_np(eps.grad), g) < 1e-10
 
 
-@pytest.mark.parametrize("tile", range(6))
+@pytest.mark.parametrize("tile", range(6))  # every entry of TILE_CFGS in csrc/fdtd.cu
 def test_every_tile_configuration(cev, tile, monkeypatch):
     """Each time-blocked tile shape (forced through CEV_FDTD_TILE) matches the
     per-step kernels on an odd-sized grid with PML, a source and probes."""
