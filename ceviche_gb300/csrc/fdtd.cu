@@ -351,6 +351,16 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
   }
   __syncthreads();
   R hx[CPT], hy[CPT], dz[CPT], ie[CPT];
+  // PML integrals of the owned cells: private to the cell, so in registers
+  // when the register budget allows (float, <= 512 threads), else in shared
+  // memory
+  constexpr bool REG_INT = NT <= 512 && sizeof(R) == 4;
+  // every owned cell lies in the same region column when NT is a multiple
+  // of the region width: its column coefficients then live in registers
+  constexpr bool COLC = (NT % RJ) == 0;
+  R ixr[REG_INT ? CPT : 1], iyr[REG_INT ? CPT : 1], idr[REG_INT ? CPT : 1];
+  // D-phase PML coefficients of the owned cells (same budget condition)
+  R dm1[REG_INT ? CPT : 1], dm2[REG_INT ? CPT : 1], dm4[REG_INT ? CPT : 1];
   unsigned srcmask = 0;  // bit k: owned cell k has a source
   unsigned pmlmask = 0;  // bit k: some cell of this warp's slot k lies on a PML row/column
 #pragma unroll
@@ -366,7 +376,11 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
       dz[k] = a.dz_i[n];
       ie[k] = a.iez[n];
       cell_pml = (xg3[r] != R(0)) | (yg3[c] != R(0)) | (xaD[r] != R(0)) | (yaD[c] != R(0));
-      if (pml) {
+      if constexpr (REG_INT) {
+        ixr[k] = pml ? a.icex_i[n] : R(0);
+        iyr[k] = pml ? a.icey_i[n] : R(0);
+        idr[k] = pml ? a.idz_i[n] : R(0);
+      } else if (pml) {
         sIx[q] = a.icex_i[n];
         sIy[q] = a.icey_i[n];
         sId[q] = a.idz_i[n];
@@ -378,6 +392,23 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
   }
   __syncthreads();
   const R S = a.S;
+  R cf1 = R(0), cf2 = R(0), cg3 = R(0), caD = R(0), cpD = R(0);
+  if constexpr (COLC) {
+    const int c0 = tid % RJ;
+    cf1 = yf1[c0]; cf2 = yf2[c0]; cg3 = yg3[c0]; caD = yaD[c0]; cpD = ypD[c0];
+  }
+  if constexpr (REG_INT) {
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+      const int q = tid + k * NT;
+      const int r = q < RN ? q / RJ : 0, c = q < RN ? q - r * RJ : 0;
+      const R ax = xaD[r], ay = yaD[c];
+      const R pd = xpD[r] * ypD[c];
+      dm1[k] = (R(1) - ax - ay - ax * ay) * pd;
+      dm2[k] = S * pd;
+      dm4[k] = R(-4) * ax * ay * pd;
+    }
+  }
   for (int st = 0; st < nst; ++st) {
     const R amp = sAmp[st];
     if (!pml) {
@@ -427,11 +458,17 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
             hx[k] = hx[k] - S * dEy;
             hy[k] = hy[k] - S * dEx;
           } else {
-            const R gx = xg3[r], gy = yg3[c];
+            const R gx = xg3[r], gy = COLC ? cg3 : yg3[c];
             R ix = R(0), iy = R(0);
-            if (gx != R(0)) { ix = sIx[q] + dEy; sIx[q] = ix; }
-            if (gy != R(0)) { iy = sIy[q] + dEx; sIy[q] = iy; }
-            hx[k] = yf1[c] * hx[k] - yf2[c] * (dEy + gx * ix);
+            if constexpr (REG_INT) {
+              if (gx != R(0)) { ixr[k] += dEy; ix = ixr[k]; }
+              if (gy != R(0)) { iyr[k] += dEx; iy = iyr[k]; }
+            } else {
+              if (gx != R(0)) { ix = sIx[q] + dEy; sIx[q] = ix; }
+              if (gy != R(0)) { iy = sIy[q] + dEx; sIy[q] = iy; }
+            }
+            const R f1c = COLC ? cf1 : yf1[c], f2c = COLC ? cf2 : yf2[c];
+            hx[k] = f1c * hx[k] - f2c * (dEy + gx * ix);
             hy[k] = xf1[r] * hy[k] - xf2[r] * (dEx + gy * iy);
           }
           sHx[q] = hx[k];
@@ -451,13 +488,28 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
           if (!(pmlmask & (1u << k))) {
             v = dz[k] + S * ch;
           } else {
-            const R ax = xaD[r], ay = yaD[c];
-            const R pd = xpD[r] * ypD[c];
-            const R m1 = (R(1) - ax - ay - ax * ay) * pd;
-            const R m2 = S * pd;
-            const R m4 = R(-4) * ax * ay * pd;
+            R m1, m2, m4;
+            if constexpr (REG_INT) {
+              m1 = dm1[k];
+              m2 = dm2[k];
+              m4 = dm4[k];
+            } else {
+              const R ax = xaD[r], ay = COLC ? caD : yaD[c];
+              const R pd = xpD[r] * (COLC ? cpD : ypD[c]);
+              m1 = (R(1) - ax - ay - ax * ay) * pd;
+              m2 = S * pd;
+              m4 = R(-4) * ax * ay * pd;
+            }
             R id = R(0);
-            if (m4 != R(0)) { id = sId[q] + dz[k]; sId[q] = id; }
+            if (m4 != R(0)) {
+              if constexpr (REG_INT) {
+                idr[k] += dz[k];
+                id = idr[k];
+              } else {
+                id = sId[q] + dz[k];
+                sId[q] = id;
+              }
+            }
             v = m1 * dz[k] + m2 * ch + m4 * id;
           }
           if (srcmask & (1u << k)) v += sW[q] * amp;
@@ -489,9 +541,15 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
         a.hy_o[n] = hy[k];
         a.dz_o[n] = dz[k];
         if (pml) {
-          a.icex_o[n] = sIx[q];
-          a.icey_o[n] = sIy[q];
-          a.idz_o[n] = sId[q];
+          if constexpr (REG_INT) {
+            a.icex_o[n] = ixr[k];
+            a.icey_o[n] = iyr[k];
+            a.idz_o[n] = idr[k];
+          } else {
+            a.icex_o[n] = sIx[q];
+            a.icey_o[n] = sIy[q];
+            a.idz_o[n] = sId[q];
+          }
         }
       }
     }
@@ -565,8 +623,9 @@ int tile_dispatch(int cfg, bool prepare, dim3 g, const TBArgs<R>& a, cudaStream_
 }
 
 // Tile choice: CEV_FDTD_TILE=<index> overrides.  Otherwise 48x48 tiles with
-// 1024 threads (measured best from 1024^2 to 4096^2), or 32x48 tiles with 512
-// threads when 48x48 tiles would not fill the GPU once (measured best at 400^2).
+// 512 threads (measured best from 1024^2 to 4096^2 once the PML integrals
+// and coefficients moved to registers), or 32x48 tiles with 512 threads when
+// 48x48 tiles would not fill the GPU once (measured best at 400^2).
 template <typename R>
 static int pick_tile(int nx, int ny) {
   auto fits = [&](int v) {
@@ -578,7 +637,7 @@ static int pick_tile(int nx, int ny) {
     if (v >= 0 && v < N_TILE_CFGS && fits(v)) return v;
   }
   const long tiles0 = (long)((nx + 47) / 48) * ((ny + 47) / 48);
-  const int order_big[] = {0, 1, 2, 5};
+  const int order_big[] = {1, 0, 2, 5};
   const int order_small[] = {2, 3, 5, 0};
   const int* order = tiles0 >= sm_count() ? order_big : order_small;
   for (int k = 0; k < 4; ++k)
