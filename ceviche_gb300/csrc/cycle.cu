@@ -1,11 +1,12 @@
-// Fused restart cycle of the stencil GMRES for one small problem.
+// Fused restart cycle of the stencil GMRES for small problems and batches.
 //
 // The multi-kernel cycle (krylov.cu) issues a matvec, a multi-dot and an
 // update launch per Arnoldi iteration, each ending in a last-block reduction
 // tail; at 200x200 (40k cells) that is launch- and latency-bound (~40 us per
 // iteration for < 1 us of memory traffic).  Here one cooperative launch runs
-// the whole cycle: every block owns a fixed set of (column tile, row chunk)
-// units for all iterations, so
+// the whole cycle for up to 16 problems, each on its own group of blocks
+// with its own barrier: every block owns a fixed set of (column tile, row
+// chunk) units of its problem for all iterations, so
 //   * the matvec of iteration j and the projections onto V_0..V_j run on the
 //     block's own cells with no barrier in between (each thread reads back
 //     only cells it wrote itself; the stencil halo of V_j, written by other
@@ -186,17 +187,25 @@ __host__ __device__ inline size_t fused_part_doubles(unsigned G, int m) {
 
 template <int POL>
 __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
-  KState* st = a.ctx.st;
+  // problem b of the batch runs on its own group of gp blocks (own barrier,
+  // partials and stage); lb is the block's index within the group
+  const int b = blockIdx.x / a.gp;
+  const unsigned lb = blockIdx.x % a.gp;
+  KState* st = a.ctx.st + b;
   if (!st->active) return;
   const int m = a.m, ny = a.ny, nx = a.nx;
-  const unsigned G = gridDim.x;
+  const unsigned G = a.gp;
   // partials as float-float pairs, [value][block] (value = 2k + re/im)
   const size_t ps = 2 * (size_t)(m + 1);
-  float2* dpart0 = (float2*)a.ctx.fpart;
+  float2* dpart0 = (float2*)(a.ctx.fpart + (size_t)b * fused_part_doubles(G, m));
   float2* dpart1 = dpart0 + (size_t)G * ps;
   float2* npart = dpart1 + (size_t)G * ps;
-  CycStage* stage = (CycStage*)(a.ctx.fpart + (size_t)fused_part_doubles(G, m));
-  unsigned* bar = a.ctx.bar;
+  CycStage* stage = (CycStage*)(a.ctx.fpart + (size_t)a.B * fused_part_doubles(G, m)) + b;
+  unsigned* bar = a.ctx.bar + 4 * b;
+  double* gsc = a.ctx.sc + (size_t)b * (m + 1);
+  const float* eps = a.eps + (size_t)b * a.eps_bs;
+  const Coef<float>* cx = a.cx + (size_t)b * nx;
+  const Coef<float>* cy = a.cy + (size_t)b * ny;
 
   __shared__ float2 sCs[64], sSnR[64], sSnI[64], sGR[65], sGI[65], sHR[66], sHI[66], sSc[65];
   __shared__ float2 sU[65];
@@ -209,26 +218,26 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
     gen = ld_volatile(bar + 1);
     sGR[0] = ff(1.f);
     sGI[0] = ff(0.f);
-    sSc[0] = ff_split(a.ctx.sc[0]);
+    sSc[0] = ff_split(gsc[0]);
     s_ok = 1;
   }
   int iters = st->iters;
   const float2 thr = ff_split(st->thresh / beta);
-  const float k2 = a.k2[0];
+  const float k2 = a.k2[b];
   __syncthreads();
 
   for (int j = 0; j < m; ++j) {
-    float2* w = a.V + (size_t)(j + 1) * a.N;
-    const float2* vj = a.V + (size_t)j * a.N;
+    float2* w = a.V + ((size_t)(j + 1) * a.B + b) * a.N;
+    const float2* vj = a.V + ((size_t)j * a.B + b) * a.N;
     // 1. w = A' (sc_j V_j) on the block's own cells
     const float s = sSc[j].x + sSc[j].y;
-    for (int u = blockIdx.x; u < a.units; u += G) {
+    for (int u = lb; u < a.units; u += G) {
       const int col = (u % a.tiles_y) * CYC_THREADS + threadIdx.x;
       if (col < ny) {
         const int i0 = (u / a.tiles_y) * a.rows, i1 = min(i0 + a.rows, nx);
         auto ep = [&](int i, float2 v, float2) { w[(size_t)i * ny + col] = cscale(v, s); };
-        stencil_column<float, POL, decltype(ep), true>(nx, ny, col, i0, i1, vj, a.eps, a.cx,
-                                                       a.cy[col], k2, ep);
+        stencil_column<float, POL, decltype(ep), true>(nx, ny, col, i0, i1, vj, eps, cx,
+                                                       cy[col], k2, ep);
       }
     }
     // 2. Gram-Schmidt passes
@@ -241,7 +250,7 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
         float2 acc[CYC_GROUP];
 #pragma unroll
         for (int k = 0; k < CYC_GROUP; ++k) acc[k] = make_float2(0.f, 0.f);
-        for (int u = blockIdx.x; u < a.units; u += G) {
+        for (int u = lb; u < a.units; u += G) {
           const int col = (u % a.tiles_y) * CYC_THREADS + threadIdx.x;
           if (col >= ny) continue;
           const int i0 = (u / a.tiles_y) * a.rows, i1 = min(i0 + a.rows, nx);
@@ -251,7 +260,8 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
             float2 v[CYC_GROUP];
 #pragma unroll
             for (int k = 0; k < CYC_GROUP; ++k)
-              v[k] = (g0 + k < nv) ? a.V[(size_t)(g0 + k) * a.N + n] : make_float2(0.f, 0.f);
+              v[k] = (g0 + k < nv) ? a.V[((size_t)(g0 + k) * a.B + b) * a.N + n]
+                                   : make_float2(0.f, 0.f);
 #pragma unroll
             for (int k = 0; k < CYC_GROUP; ++k) {
               acc[k].x += v[k].x * wv.x + v[k].y * wv.y;
@@ -267,7 +277,7 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
         }
         const float2 tot = block_sum_ff<2 * CYC_GROUP>(fv, smf);
         if (threadIdx.x < 2 * CYC_GROUP && g0 + (int)(threadIdx.x >> 1) < nv)
-          dpart[(size_t)(2 * g0 + threadIdx.x) * G + blockIdx.x] = tot;
+          dpart[(size_t)(2 * g0 + threadIdx.x) * G + lb] = tot;
         __syncthreads();
       }
       if (!grid_sync(bar, G, gen, &s_ok, st)) return;
@@ -293,7 +303,7 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
       __syncthreads();
       // w -= sum_k V_k u_k on the block's own cells
       const bool last = pass == npass - 1;
-      for (int u = blockIdx.x; u < a.units; u += G) {
+      for (int u = lb; u < a.units; u += G) {
         const int col = (u % a.tiles_y) * CYC_THREADS + threadIdx.x;
         if (col >= ny) continue;
         const int i0 = (u / a.tiles_y) * a.rows, i1 = min(i0 + a.rows, nx);
@@ -305,7 +315,8 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
             float2 v[GL];
 #pragma unroll
             for (int k = 0; k < GL; ++k)
-              v[k] = (k0 + k < nv) ? a.V[(size_t)(k0 + k) * a.N + n] : make_float2(0.f, 0.f);
+              v[k] = (k0 + k < nv) ? a.V[((size_t)(k0 + k) * a.B + b) * a.N + n]
+                                   : make_float2(0.f, 0.f);
 #pragma unroll
             for (int k = 0; k < GL; ++k) {
               const float2 c = (k0 + k < nv) ? sU[k0 + k] : make_float2(0.f, 0.f);
@@ -322,7 +333,7 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
     {
       float accf[1] = {nrm};
       const float2 tot = block_sum_ff<1>(accf, smf);
-      if (threadIdx.x == 0) npart[blockIdx.x] = tot;
+      if (threadIdx.x == 0) npart[lb] = tot;
     }
     if (!grid_sync(bar, G, gen, &s_ok, st)) return;
     if (threadIdx.x < 32) {
@@ -382,7 +393,7 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
       const bool bad = !isfinite(res.x) || !isfinite(hn.x);
       const bool stop = bad || ff_le(res, thr) || breakdown || j + 1 >= m || iters >= a.ctx.max_iters;
       s_active = stop ? 0 : 1;
-      if (blockIdx.x == 0) {
+      if (lb == 0) {
         stage->res = res;
         st->ncols = j + 1;
         st->iters = iters;
@@ -391,7 +402,7 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
       }
     }
     __syncthreads();
-    if (blockIdx.x == 0) {  // stage column j and the rotation (parallel stores)
+    if (lb == 0) {  // stage column j and the rotation (parallel stores)
       for (int k = threadIdx.x; k <= j + 1; k += blockDim.x) {
         stage->H[((size_t)j * 65 + k) * 2] = sHR[k];
         stage->H[((size_t)j * 65 + k) * 2 + 1] = sHI[k];
@@ -411,11 +422,19 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
   }
 }
 
-// FP64 Krylov arrays from the staged float-float results (one block).
-__global__ void k_cycle_publish(KCtx c, int m, const CycStage* stage) {
-  const KState* st = c.st;
+// FP64 Krylov arrays from the staged float-float results (one block per
+// problem).
+__global__ void k_cycle_publish(KCtx c, int m, const CycStage* stages) {
+  const int b = blockIdx.x;
+  const KState* st = c.st + b;
+  const CycStage* stage = stages + b;
   const int nc = st->ncols;
   if (nc == 0) return;
+  c.H += (size_t)b * m * (m + 1);
+  c.cs += (size_t)b * m;
+  c.sn += (size_t)b * m;
+  c.gam += (size_t)b * (m + 1);
+  c.sc += (size_t)b * (m + 1);
   const double beta = st->beta;
   for (int e = threadIdx.x; e < nc * (m + 1); e += blockDim.x) {
     const int col = e / (m + 1), k = e % (m + 1);
@@ -431,13 +450,16 @@ __global__ void k_cycle_publish(KCtx c, int m, const CycStage* stage) {
     c.gam[k] = make_double2(beta * ff_d(stage->gam[2 * k]), beta * ff_d(stage->gam[2 * k + 1]));
     if (k > 0) c.sc[k] = ff_d(stage->sc[k]);
   }
-  if (threadIdx.x == 0) c.st->res_est = beta * ff_d(stage->res);
+  if (threadIdx.x == 0) c.st[b].res_est = beta * ff_d(stage->res);
 }
 
-// Grid of the fused cycle: units of CYC_THREADS columns x rows rows, about
-// as many as co-resident blocks (at most 2 per SM); 0 if unavailable.
-// limit > 0 caps the blocks further (blocks then loop over several units).
-int cycle_plan(int nx, int ny, int pol, int limit, int& rows, int& tiles_y, int& units) {
+// Grid of the fused cycle for a batch of B problems: a group of gp blocks per
+// problem, each block a set of units of CYC_THREADS columns x rows rows, all
+// groups together about as many blocks as are co-resident (at most 2 per SM).
+// limit > 0 caps gp (blocks then loop over several units).  Returns the total
+// number of blocks, 0 if the fused cycle is not available.
+int cycle_plan(int nx, int ny, int pol, int B, int limit, int& rows, int& tiles_y, int& units,
+               int& gp) {
   static int coop = -1;
   if (coop < 0) {
     int dev = 0, v = 0;
@@ -445,7 +467,7 @@ int cycle_plan(int nx, int ny, int pol, int limit, int& rows, int& tiles_y, int&
     cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, dev);
     coop = v;
   }
-  if (!coop) return 0;
+  if (!coop || B < 1) return 0;
   int per_sm = 0;
   if (pol == POL_EZ)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cycle<POL_EZ>, CYC_THREADS, 0);
@@ -453,11 +475,14 @@ int cycle_plan(int nx, int ny, int pol, int limit, int& rows, int& tiles_y, int&
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cycle<POL_HZ>, CYC_THREADS, 0);
   if (per_sm < 1) return 0;
   const int cap = std::min(fused_max_blocks(), std::min(per_sm, 2) * sm_count());
+  const int per = cap / B;  // blocks per problem
+  if (per < 1) return 0;
   tiles_y = (ny + CYC_THREADS - 1) / CYC_THREADS;
-  rows = std::max(1, (int)(((long)nx * tiles_y + cap - 1) / cap));
+  rows = std::max(1, (int)(((long)nx * tiles_y + per - 1) / per));
   units = tiles_y * ((nx + rows - 1) / rows);
-  const int g = std::min(units, cap);
-  return limit > 0 ? std::min(g, limit) : g;
+  gp = std::min(units, per);
+  if (limit > 0) gp = std::min(gp, limit);
+  return gp * B;
 }
 
 int cycle_launch(int pol, int blocks, const CycArgs& a, cudaStream_t s) {
@@ -470,8 +495,9 @@ int cycle_launch(int pol, int blocks, const CycArgs& a, cudaStream_t s) {
     e = cudaLaunchCooperativeKernel((const void*)k_cycle<POL_HZ>, dim3(blocks), dim3(CYC_THREADS),
                                     args, 0, s);
   if (e != cudaSuccess) return cuda_status(e, "k_cycle");
-  const CycStage* stage = (const CycStage*)(a.ctx.fpart + fused_part_doubles(blocks, a.m));
-  k_cycle_publish<<<1, 256, 0, s>>>(a.ctx, a.m, stage);
+  const CycStage* stages =
+      (const CycStage*)(a.ctx.fpart + (size_t)a.B * fused_part_doubles(a.gp, a.m));
+  k_cycle_publish<<<a.B, 256, 0, s>>>(a.ctx, a.m, stages);
   CEV_CHECK_LAUNCH("k_cycle_publish");
   return CEV_OK;
 }

@@ -27,8 +27,8 @@ namespace cev {
 void launch_geometry(int nx, int ny, int batch, dim3& grid, dim3& block, int& rows);
 
 static constexpr int DOT_GROUP = 16;
-// Largest single problem solved with the fused cycle; above it the
-// per-iteration launches are bandwidth-bound and their overhead small.
+// Largest batch (cells over all problems) solved with the fused cycle; above
+// it the per-iteration launches are bandwidth-bound and their overhead small.
 static constexpr size_t FUSED_MAX_CELLS = (size_t)1 << 21;
 
 // --------------------------------------------------------------- residual
@@ -457,7 +457,7 @@ KLayout klayout(const KrylovProblem& P, const cev_solve_opts& o, size_t pc_bytes
   L.V = take(sizeof(float2) * N * B * (m + 1));
   L.Z = take(o.precond != CEV_PRECOND_NONE ? sizeof(float2) * N * B * m : 0);
   L.partial = take(sizeof(double) * L.part_stride * B);
-  L.counter = take(sizeof(unsigned) * (2 * B + 4));  // + fused-cycle barrier words
+  L.counter = take(sizeof(unsigned) * (2 * B + 4 * B));  // + fused-cycle barrier words
   L.st = take(sizeof(KState) * B);
   L.H = take(sizeof(double2) * (size_t)B * m * (m + 1));
   L.cs = take(sizeof(double) * (size_t)B * m);
@@ -466,10 +466,12 @@ KLayout klayout(const KrylovProblem& P, const cev_solve_opts& o, size_t pc_bytes
   L.sc = take(sizeof(double) * (size_t)B * (m + 1));
   L.y = take(sizeof(double2) * (size_t)B * m);
   L.hpass = take(sizeof(double2) * (size_t)B * (m + 1));
-  // fused cycle (single problem): two dot-pass regions and the norm partials
-  L.fpart = take(B == 1 ? sizeof(double) * (size_t)fused_max_blocks() * (4 * (m + 1) + 1) +
-                              cycle_stage_bytes()
-                        : 0);
+  // fused cycle (<= FUSED_MAX_BATCH problems): per problem two dot-pass
+  // regions and the norm partials, then one stage per problem
+  L.fpart = take(B <= FUSED_MAX_BATCH
+                     ? sizeof(double) * (size_t)fused_max_blocks() * (4 * (m + 1) + 1) +
+                           (size_t)B * cycle_stage_bytes()
+                     : 0);
   L.pc = off;
   off = align256(off + pc_bytes);
   L.total = off;
@@ -519,8 +521,8 @@ int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opt
   float2* Z = (float2*)(w + L.Z);
   CEV_REQUIRE(!flexible || ops.precond, "preconditioner not available for this operator");
 
-  CEV_CUDA(cudaMemsetAsync(c.counter, 0, sizeof(unsigned) * (2 * B + 4), s));
-  const bool fused = ops.cycle && !flexible && B == 1;
+  CEV_CUDA(cudaMemsetAsync(c.counter, 0, sizeof(unsigned) * (2 * B + 4 * B), s));
+  const bool fused = ops.cycle && !flexible && B <= FUSED_MAX_BATCH;
   CEV_CUDA(cudaMemsetAsync(c.st, 0, sizeof(KState) * B, s));
   if (!o.use_x0)
     k_zero_c128<<<std::min(ceil_div(N * B, 256), 8u * sm_count()), 256, 0, s>>>(xvec, N * B);
@@ -571,7 +573,7 @@ int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opt
       CEV_CUDA(cudaMemcpyAsync(c.st, hst.data(), sizeof(KState) * B, cudaMemcpyHostToDevice, s));
     if (!any) break;
     if (fused) {
-      CEV_CUDA(cudaMemsetAsync(c.bar, 0, sizeof(unsigned) * 4, s));
+      CEV_CUDA(cudaMemsetAsync(c.bar, 0, sizeof(unsigned) * 4 * B, s));
       if ((rc = ops.cycle(c, V, s)) != CEV_OK) return rc;
     }
     for (int j = 0; j < (fused ? 0 : m); ++j) {
@@ -706,20 +708,20 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
     CEV_CHECK_LAUNCH("k_arnoldi_mv");
     return CEV_OK;
   };
-  // One launch per restart cycle for a single small problem (the per-
-  // iteration launches are latency-bound there).  CEV_FUSED_CYCLE=0 disables
+  // One launch per restart cycle for a small batch (the per-iteration
+  // launches are latency-bound there).  CEV_FUSED_CYCLE=0 disables
   // it; CEV_FUSED_BLOCKS=<n> caps its blocks (testing the multi-unit loop).
-  int cyc_rows = 0, cyc_tiles = 0, cyc_units = 0, cyc_blocks = 0;
+  int cyc_rows = 0, cyc_tiles = 0, cyc_units = 0, cyc_gp = 0, cyc_blocks = 0;
   const char* fenv = std::getenv("CEV_FUSED_CYCLE");
   const char* benv = std::getenv("CEV_FUSED_BLOCKS");
-  if (!(fenv && fenv[0] == '0') && B == 1 && o.precond == CEV_PRECOND_NONE &&
-      N <= FUSED_MAX_CELLS)
-    cyc_blocks = cycle_plan(p->nx, p->ny, p->pol, benv ? std::atoi(benv) : 0, cyc_rows,
-                            cyc_tiles, cyc_units);
+  if (!(fenv && fenv[0] == '0') && B <= FUSED_MAX_BATCH && o.precond == CEV_PRECOND_NONE &&
+      N * B <= FUSED_MAX_CELLS)
+    cyc_blocks = cycle_plan(p->nx, p->ny, p->pol, B, benv ? std::atoi(benv) : 0, cyc_rows,
+                            cyc_tiles, cyc_units, cyc_gp);
   if (cyc_blocks > 0) {
     ops.cycle = [&](const KCtx& c, float2* V, cudaStream_t st) -> int {
-      CycArgs a{p->nx, p->ny, cyc_rows, m, o.reorth, cyc_tiles, cyc_units, N, eps32,
-                p->cx32[tr], p->cy32[tr], p->k2_32, V, c};
+      CycArgs a{p->nx, p->ny, cyc_rows, m, o.reorth, cyc_tiles, cyc_units, B, cyc_gp, N,
+                eps_shared ? 0 : N, eps32, p->cx32[tr], p->cy32[tr], p->k2_32, V, c};
       return cycle_launch(p->pol, cyc_blocks, a, st);
     };
   }

@@ -68,16 +68,18 @@ struct KrylovOps {
   std::function<int(const KCtx&, int j, const float2* in, int use_scale, float2* out,
                     cudaStream_t)> matvec;
   std::function<int(const KCtx&, int j, const float2* v, float2* z, cudaStream_t)> precond;
-  // Optional: the whole Arnoldi cycle of an unpreconditioned single problem
-  // in one launch (replaces the per-iteration matvec / dot / update launches).
+  // Optional: the whole Arnoldi cycle of an unpreconditioned small batch in
+  // one launch (replaces the per-iteration matvec / dot / update launches).
   std::function<int(const KCtx&, float2* V, cudaStream_t)> cycle;
   double bscale = 1.0;
 };
 
-// Fused single-problem stencil cycle (cycle.cu).
+// Fused stencil cycle for small batches (cycle.cu).
 struct CycArgs {
   int nx, ny, rows, m, reorth, tiles_y, units;
+  int B, gp;      // problems, blocks per problem
   size_t N;
+  size_t eps_bs;  // eps batch stride (0: shared)
   const float* eps;
   const Coef<float>* cx;
   const Coef<float>* cy;
@@ -87,9 +89,11 @@ struct CycArgs {
 };
 int fused_max_blocks();
 size_t cycle_stage_bytes();
-// Blocks of the fused cycle for an nx x ny grid (0: not available) and its
-// work split; limit > 0 caps the blocks (each then loops over several units).
-int cycle_plan(int nx, int ny, int pol, int limit, int& rows, int& tiles_y, int& units);
+// Blocks of the fused cycle for B problems on an nx x ny grid (0: not
+// available), its work split and gp blocks per problem; limit > 0 caps gp.
+int cycle_plan(int nx, int ny, int pol, int B, int limit, int& rows, int& tiles_y, int& units,
+               int& gp);
+static constexpr int FUSED_MAX_BATCH = 16;
 int cycle_launch(int pol, int blocks, const CycArgs& a, cudaStream_t s);
 
 int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opts& o,

@@ -261,3 +261,32 @@ def test_fused_cycle_matches_multikernel(cev, pol, reorth, shape, blocks, monkey
         (xf, itf), (xm, itm) = out["fused", tr], out["multi", tr]
         assert _rel(xf, xm) < 1e-5, (itf, itm)
         assert abs(itf - itm) <= 0.1 * itm + 2, (itf, itm)
+
+
+@pytest.mark.parametrize("shared_eps", [True, False])
+def test_fused_cycle_batch(cev, shared_eps, monkeypatch):
+    """A batch of 5 problems through the fused cycle (one block group per
+    problem, problems converging at different iterations) against the
+    per-iteration launch path."""
+    from ceviche_gb300 import primitives as P
+    rng = np.random.default_rng(23)
+    Nx, Ny, dL, npml = 64, 52, 40e-9, [8, 8]
+    oms = 2 * np.pi * 3e8 / np.array([1.3e-6, 1.45e-6, 1.55e-6, 1.7e-6, 1.9e-6])
+    B = len(oms)
+    eps = rng.uniform(1, 5, (Nx, Ny)) if shared_eps else rng.uniform(1, 5, (B, Nx, Ny))
+    b = rng.standard_normal((B, Nx, Ny)) + 1j * rng.standard_normal((B, Nx, Ny))
+    plan = P.get_plan("ez", (Nx, Ny), dL, oms, npml)
+    out = {}
+    for mode in ("fused", "multi"):
+        if mode == "multi":
+            monkeypatch.setenv("CEV_FUSED_CYCLE", "0")
+        x, info = P.solve(plan, torch.as_tensor(eps), torch.as_tensor(b), tol=1e-8, strict=True)
+        out[mode] = (x.cpu().numpy(), [i["iterations"] for i in info])
+        for k, w in enumerate(oms):
+            A = ofd.make_A("ez", w, dL, eps if shared_eps else eps[k], npml)
+            assert ofd.true_residual(A, out[mode][0][k].ravel(), b[k].ravel()) < 1e-8
+    (xf, itf), (xm, itm) = out["fused"], out["multi"]
+    assert _rel(xf, xm) < 1e-6, (itf, itm)
+    assert len(set(itf)) > 1  # the problems really finish at different iterations
+    for a_, b_ in zip(itf, itm):
+        assert abs(a_ - b_) <= 0.1 * b_ + 2, (itf, itm)
