@@ -59,6 +59,7 @@ SIGNATURES = {
     "cev_version": (I, []),
     "cev_fdfd_plan_create": (I, [PP, I, I, I, I, D, C.POINTER(C.c_double), I, I, D, D]),
     "cev_fdfd_plan_destroy": (I, [P]),
+    "cev_fdfd_plan_set_eps_complex": (I, [P, I]),
     "cev_fdfd_plan_scale": (D, [P]),
     "cev_fdfd_apply": (I, [P, P, I, P, P, I, I, I, P]),
     "cev_solve_opts_default": (None, [C.POINTER(SolveOpts)]),

@@ -185,7 +185,7 @@ __host__ __device__ inline size_t fused_part_doubles(unsigned G, int m) {
   return 2 * (size_t)G * 2 * (size_t)(m + 1) + G;
 }
 
-template <int POL>
+template <int POL, typename E>
 __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
   // problem b of the batch runs on its own group of gp blocks (own barrier,
   // partials and stage); lb is the block's index within the group
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
   CycStage* stage = (CycStage*)(a.ctx.fpart + (size_t)a.B * fused_part_doubles(G, m)) + b;
   unsigned* bar = a.ctx.bar + 4 * b;
   double* gsc = a.ctx.sc + (size_t)b * (m + 1);
-  const float* eps = a.eps + (size_t)b * a.eps_bs;
+  const E* eps = (const E*)a.eps + (size_t)b * a.eps_bs;
   const Coef<float>* cx = a.cx + (size_t)b * nx;
   const Coef<float>* cy = a.cy + (size_t)b * ny;
 
@@ -236,8 +236,8 @@ __global__ void __launch_bounds__(CYC_THREADS) k_cycle(CycArgs a) {
       if (col < ny) {
         const int i0 = (u / a.tiles_y) * a.rows, i1 = min(i0 + a.rows, nx);
         auto ep = [&](int i, float2 v, float2) { w[(size_t)i * ny + col] = cscale(v, s); };
-        stencil_column<float, POL, decltype(ep), true>(nx, ny, col, i0, i1, vj, eps, cx,
-                                                       cy[col], k2, ep);
+        stencil_column<float, POL, decltype(ep), true, E>(nx, ny, col, i0, i1, vj, eps, cx,
+                                                          cy[col], k2, ep);
       }
     }
     // 2. Gram-Schmidt passes
@@ -458,8 +458,15 @@ __global__ void k_cycle_publish(KCtx c, int m, const CycStage* stages) {
 // groups together about as many blocks as are co-resident (at most 2 per SM).
 // limit > 0 caps gp (blocks then loop over several units).  Returns the total
 // number of blocks, 0 if the fused cycle is not available.
-int cycle_plan(int nx, int ny, int pol, int B, int limit, int& rows, int& tiles_y, int& units,
-               int& gp) {
+template <int POL, typename E>
+static int cycle_occupancy() {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cycle<POL, E>, CYC_THREADS, 0);
+  return per_sm;
+}
+
+int cycle_plan(int nx, int ny, int pol, int ceps, int B, int limit, int& rows, int& tiles_y,
+               int& units, int& gp) {
   static int coop = -1;
   if (coop < 0) {
     int dev = 0, v = 0;
@@ -468,11 +475,10 @@ int cycle_plan(int nx, int ny, int pol, int B, int limit, int& rows, int& tiles_
     coop = v;
   }
   if (!coop || B < 1) return 0;
-  int per_sm = 0;
-  if (pol == POL_EZ)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cycle<POL_EZ>, CYC_THREADS, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cycle<POL_HZ>, CYC_THREADS, 0);
+  const int per_sm = pol == POL_EZ ? (ceps ? cycle_occupancy<POL_EZ, float2>()
+                                             : cycle_occupancy<POL_EZ, float>())
+                                   : (ceps ? cycle_occupancy<POL_HZ, float2>()
+                                           : cycle_occupancy<POL_HZ, float>());
   if (per_sm < 1) return 0;
   const int cap = std::min(fused_max_blocks(), std::min(per_sm, 2) * sm_count());
   const int per = cap / B;  // blocks per problem
@@ -485,15 +491,14 @@ int cycle_plan(int nx, int ny, int pol, int B, int limit, int& rows, int& tiles_
   return gp * B;
 }
 
-int cycle_launch(int pol, int blocks, const CycArgs& a, cudaStream_t s) {
+int cycle_launch(int pol, int ceps, int blocks, const CycArgs& a, cudaStream_t s) {
   void* args[] = {(void*)&a};
-  cudaError_t e;
-  if (pol == POL_EZ)
-    e = cudaLaunchCooperativeKernel((const void*)k_cycle<POL_EZ>, dim3(blocks), dim3(CYC_THREADS),
-                                    args, 0, s);
-  else
-    e = cudaLaunchCooperativeKernel((const void*)k_cycle<POL_HZ>, dim3(blocks), dim3(CYC_THREADS),
-                                    args, 0, s);
+  const void* fn = pol == POL_EZ ? (ceps ? (const void*)k_cycle<POL_EZ, float2>
+                                         : (const void*)k_cycle<POL_EZ, float>)
+                                 : (ceps ? (const void*)k_cycle<POL_HZ, float2>
+                                         : (const void*)k_cycle<POL_HZ, float>);
+  const cudaError_t e =
+      cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(CYC_THREADS), args, 0, s);
   if (e != cudaSuccess) return cuda_status(e, "k_cycle");
   const CycStage* stages =
       (const CycStage*)(a.ctx.fpart + (size_t)a.B * fused_part_doubles(a.gp, a.m));

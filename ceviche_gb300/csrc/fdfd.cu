@@ -97,10 +97,10 @@ void axis_tables(int pol, int N, int npml, double dL, double omega, double phase
 }
 
 // ------------------------------------------------------------ apply kernel
-template <typename R>
+template <typename R, typename E = R>
 struct ApplyArgs {
   int nx, ny, batch, rows;
-  const R* eps;
+  const E* eps;
   size_t eps_bs;
   const Cplx<R>* x;
   Cplx<R>* y;
@@ -110,8 +110,8 @@ struct ApplyArgs {
   R oscale;
 };
 
-template <typename R, int POL>
-__global__ void __launch_bounds__(128) k_apply(ApplyArgs<R> a) {
+template <typename R, int POL, typename E>
+__global__ void __launch_bounds__(128) k_apply(ApplyArgs<R, E> a) {
   using C = Cplx<R>;
   const int b = blockIdx.z;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -121,11 +121,12 @@ __global__ void __launch_bounds__(128) k_apply(ApplyArgs<R> a) {
   const size_t N = (size_t)a.nx * a.ny;
   const C* x = a.x + b * N;
   C* y = a.y + b * N;
-  const R* eps = a.eps + b * a.eps_bs;
+  const E* eps = a.eps + b * a.eps_bs;
   const Coef<R> cyj = a.cy[(size_t)b * a.ny + j];
   const R os = a.oscale;
   auto ep = [&](int i, C v, C) { y[(size_t)i * a.ny + j] = cscale(v, os); };
-  stencil_column<R, POL>(a.nx, a.ny, j, i0, i1, x, eps, a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
+  stencil_column<R, POL, decltype(ep), false, E>(a.nx, a.ny, j, i0, i1, x, eps,
+                                                 a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
 }
 
 void launch_geometry(int nx, int ny, int batch, dim3& grid, dim3& block, int& rows) {
@@ -138,11 +139,11 @@ void launch_geometry(int nx, int ny, int batch, dim3& grid, dim3& block, int& ro
   grid = dim3(cols, (nx + rows - 1) / rows, batch);
 }
 
-template <typename R>
-static int apply_impl(cev_fdfd_plan p, const R* eps, int eps_shared, const Cplx<R>* x, Cplx<R>* y,
+template <typename R, typename E>
+static int apply_impl(cev_fdfd_plan p, const E* eps, int eps_shared, const Cplx<R>* x, Cplx<R>* y,
                       int transpose, const Coef<R>* cx, const Coef<R>* cy, const R* k2, R oscale,
                       cudaStream_t s) {
-  ApplyArgs<R> a;
+  ApplyArgs<R, E> a;
   a.nx = p->nx;
   a.ny = p->ny;
   a.batch = p->batch;
@@ -157,17 +158,31 @@ static int apply_impl(cev_fdfd_plan p, const R* eps, int eps_shared, const Cplx<
   dim3 grid, block;
   launch_geometry(p->nx, p->ny, p->batch, grid, block, a.rows);
   if (p->pol == POL_EZ)
-    k_apply<R, POL_EZ><<<grid, block, 0, s>>>(a);
+    k_apply<R, POL_EZ, E><<<grid, block, 0, s>>>(a);
   else
-    k_apply<R, POL_HZ><<<grid, block, 0, s>>>(a);
+    k_apply<R, POL_HZ, E><<<grid, block, 0, s>>>(a);
   CEV_CHECK_LAUNCH("k_apply");
   return CEV_OK;
 }
 
 // -------------------------------------------------------- field conversion
+// Permittivity elements: E = double (real eps) or double2 (complex eps,
+// lossy media, interleaved).  The field and gradient kernels below compute in
+// complex arithmetic throughout; for real eps every imaginary part is an
+// exact zero, so the results equal the real-arithmetic ones.
+__device__ __forceinline__ double2 ldE(const double* e, size_t i) { return make_double2(e[i], 0.0); }
+__device__ __forceinline__ double2 ldE(const double2* e, size_t i) { return e[i]; }
+// geps accumulation of a complex sensitivity c = dL-linear coefficient of
+// d eps: real eps takes Re(c); complex eps (PyTorch convention
+// dL/dRe + i dL/dIm) takes conj(c).
+__device__ __forceinline__ void gacc(double* g, size_t i, double2 c) { g[i] += c.x; }
+__device__ __forceinline__ void gacc(double2* g, size_t i, double2 c) { g[i] = cadd(g[i], cconj(c)); }
+// 1 / ((a + b)/2 + 1e-5) in complex arithmetic
+__device__ __forceinline__ double2 hz_dc(double2 a, double2 b) { return hz_d(a, b); }
+
 struct FieldArgs {
   int nx, ny, batch;
-  const double* eps;
+  const void* eps;
   size_t eps_bs;
   const double2* fz;
   double2* f1;
@@ -203,6 +218,7 @@ __global__ void k_fields_ez(FieldArgs a) {
 }
 
 // Hz -> (Ex, Ey) = (Dyf Hz / (eps_xx+1e-5), -Dxf Hz / (eps_yy+1e-5)) / (1j w eps0)
+template <typename E>
 __global__ void k_fields_hz(FieldArgs a) {
   const size_t N = (size_t)a.nx * a.ny;
   const int b = blockIdx.y;
@@ -210,7 +226,7 @@ __global__ void k_fields_hz(FieldArgs a) {
        n += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(n / a.ny), j = (int)(n % a.ny);
     const double2* u = a.fz + b * N;
-    const double* e = a.eps + b * a.eps_bs;
+    const E* e = (const E*)a.eps + b * a.eps_bs;
     const double2 uc = u[n];
     double2 up_x = u[(size_t)((i + 1) % a.nx) * a.ny + j];
     double2 up_y = u[(size_t)i * a.ny + (j + 1) % a.ny];
@@ -218,27 +234,25 @@ __global__ void k_fields_hz(FieldArgs a) {
     if (j == a.ny - 1) up_y = cmul(a.phy, up_y);
     const double2 dxf = cscale(cmul(a.sfx[(size_t)b * a.nx + i], csub(up_x, uc)), 1.0 / a.dL);
     const double2 dyf = cscale(cmul(a.sfy[(size_t)b * a.ny + j], csub(up_y, uc)), 1.0 / a.dL);
-    const double ec = e[n];
-    const double exx = 0.5 * (ec + e[(size_t)i * a.ny + (j + a.ny - 1) % a.ny]) + 1e-5;
-    const double eyy = 0.5 * (ec + e[(size_t)((i + a.nx - 1) % a.nx) * a.ny + j]) + 1e-5;
+    const double2 ec = ldE(e, n);
+    const double2 dxx = hz_dc(ec, ldE(e, (size_t)i * a.ny + (j + a.ny - 1) % a.ny));
+    const double2 dyy = hz_dc(ec, ldE(e, (size_t)((i + a.nx - 1) % a.nx) * a.ny + j));
     const double c = 1.0 / (a.omega[b] * EPSILON_0);
     // 1/(1j w eps0) = -1j c
-    const double2 ex = cscale(make_double2(c * dyf.y, -c * dyf.x), 1.0 / exx);
-    const double2 ey = cscale(make_double2(-c * dxf.y, c * dxf.x), 1.0 / eyy);
-    a.f1[b * N + n] = ex;
-    a.f2[b * N + n] = ey;
+    a.f1[b * N + n] = cmul(make_double2(c * dyf.y, -c * dyf.x), dxx);
+    a.f2[b * N + n] = cmul(make_double2(-c * dxf.y, c * dxf.x), dyy);
   }
 }
 
 // ------------------------------------------------- field conversion adjoint
 struct FieldAdjArgs {
   int nx, ny, batch, eps_shared;
-  const double* eps;
+  const void* eps;
   const double2* fz;
   const double2* g1;
   const double2* g2;
   double2* gz;
-  double* geps;
+  void* geps;
   const double2 *sfx, *sbx, *sfy, *sby;
   double2 phx, phy;
   const double* omega;
@@ -277,9 +291,9 @@ __global__ void k_fields_adj_ez(FieldAdjArgs a) {
   }
 }
 
-// Hz: Ex = be*dxx*Dyf Hz, Ey = -be*dyy*Dxf Hz, be = -1j c, c = 1/(w eps0)
-__device__ __forceinline__ double hz_dd(double a, double b) { return 1.0 / (0.5 * (a + b) + 1e-5); }
-
+// Hz: Ex = be*dxx*Dyf Hz, Ey = -be*dyy*Dxf Hz, be = -1j c, c = 1/(w eps0);
+// gz += Dyf^H conj(be dxx) g1 + Dxf^H conj(-be dyy) g2
+template <typename E>
 __global__ void k_fields_adj_hz(FieldAdjArgs a) {
   const size_t N = (size_t)a.nx * a.ny;
   const int b = blockIdx.y;
@@ -288,22 +302,24 @@ __global__ void k_fields_adj_hz(FieldAdjArgs a) {
        n += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(n / a.ny), j = (int)(n % a.ny);
     const int im = (i + a.nx - 1) % a.nx, jm = (j + a.ny - 1) % a.ny;
-    const double* e = a.eps + b * ebs;
+    const E* e = (const E*)a.eps + b * ebs;
     const double c = 1.0 / (a.omega[b] * EPSILON_0);
     const double2* g1 = a.g1 + b * N;
     const double2* g2 = a.g2 + b * N;
     const double2* sfx = a.sfx + (size_t)b * a.nx;
     const double2* sfy = a.sfy + (size_t)b * a.ny;
-    // v1 = conj(be) dxx g1 = 1j c dxx g1 ; v2 = conj(-be) dyy g2 = -1j c dyy g2
+    // v1 = conj(be) conj(dxx) g1 = 1j c conj(dxx) g1 ; v2 = -1j c conj(dyy) g2
     auto v1 = [&](int ii, int jj) {
-      const double d = hz_dd(e[(size_t)ii * a.ny + jj], e[(size_t)ii * a.ny + (jj + a.ny - 1) % a.ny]);
-      const double2 g = g1[(size_t)ii * a.ny + jj];
-      return make_double2(-c * d * g.y, c * d * g.x);
+      const double2 d = hz_dc(ldE(e, (size_t)ii * a.ny + jj),
+                              ldE(e, (size_t)ii * a.ny + (jj + a.ny - 1) % a.ny));
+      const double2 g = cmulc(d, g1[(size_t)ii * a.ny + jj]);
+      return make_double2(-c * g.y, c * g.x);
     };
     auto v2 = [&](int ii, int jj) {
-      const double d = hz_dd(e[(size_t)ii * a.ny + jj], e[(size_t)((ii + a.nx - 1) % a.nx) * a.ny + jj]);
-      const double2 g = g2[(size_t)ii * a.ny + jj];
-      return make_double2(c * d * g.y, -c * d * g.x);
+      const double2 d = hz_dc(ldE(e, (size_t)ii * a.ny + jj),
+                              ldE(e, (size_t)((ii + a.nx - 1) % a.nx) * a.ny + jj));
+      const double2 g = cmulc(d, g2[(size_t)ii * a.ny + jj]);
+      return make_double2(c * g.y, -c * g.x);
     };
     // (Dyf^H v)_k = (-conj(sf_k) v_k + conj(sf_{k-1}) v_{k-1} [conj(ph) at k=0]) / dL
     double2 q = cmulc(sfy[jm], v1(i, jm));
@@ -318,7 +334,9 @@ __global__ void k_fields_adj_hz(FieldAdjArgs a) {
   }
 }
 
-// direct eps dependence of (Ex, Ey): geps += avg^T( -d^2 Re(conj(g) * coef * Df Hz) )
+// Direct eps dependence of (Ex, Ey): sensitivity of L to d is conj(g) * coef
+// * Df Hz; d = 1/(avg + 1e-5) so d d = -d^2 d avg; avg^T spreads it to eps.
+template <typename E, typename G>
 __global__ void k_fields_adj_hz_eps(FieldAdjArgs a) {
   const size_t N = (size_t)a.nx * a.ny;
   const int nb = a.eps_shared ? a.batch : 1;
@@ -327,15 +345,14 @@ __global__ void k_fields_adj_hz_eps(FieldAdjArgs a) {
        n += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(n / a.ny), j = (int)(n % a.ny);
     const int ip = (i + 1) % a.nx, jp = (j + 1) % a.ny;
-    double acc = 0.0;
+    double2 acc = make_double2(0.0, 0.0);
     for (int bb = 0; bb < nb; ++bb) {
       const int b = b0 + bb;
-      const double* e = a.eps + (a.eps_shared ? 0 : b * N);
+      const E* e = (const E*)a.eps + (a.eps_shared ? 0 : b * N);
       const double2* u = a.fz + b * N;
       const double c = 1.0 / (a.omega[b] * EPSILON_0);
       const double2* sfx = a.sfx + (size_t)b * a.nx;
       const double2* sfy = a.sfy + (size_t)b * a.ny;
-      // t_xx(i,j) = -dxx^2 Re(conj(g1) * (-1j c) * Dyf u)
       auto txx = [&](int ii, int jj) {
         const size_t m = (size_t)ii * a.ny + jj;
         const int jj1 = (jj + 1) % a.ny;
@@ -343,9 +360,8 @@ __global__ void k_fields_adj_hz_eps(FieldAdjArgs a) {
         if (jj == a.ny - 1) up = cmul(a.phy, up);
         const double2 df = cscale(cmul(sfy[jj], csub(up, u[m])), 1.0 / a.dL);
         const double2 ex_c = make_double2(c * df.y, -c * df.x);  // (-1j c) df
-        const double2 g = a.g1[b * N + m];
-        const double d = hz_dd(e[m], e[(size_t)ii * a.ny + (jj + a.ny - 1) % a.ny]);
-        return -d * d * (g.x * ex_c.x + g.y * ex_c.y);
+        const double2 d = hz_dc(ldE(e, m), ldE(e, (size_t)ii * a.ny + (jj + a.ny - 1) % a.ny));
+        return cscale(cmul(cmul(d, d), cmulc(a.g1[b * N + m], ex_c)), -1.0);
       };
       auto tyy = [&](int ii, int jj) {
         const size_t m = (size_t)ii * a.ny + jj;
@@ -354,32 +370,34 @@ __global__ void k_fields_adj_hz_eps(FieldAdjArgs a) {
         if (ii == a.nx - 1) up = cmul(a.phx, up);
         const double2 df = cscale(cmul(sfx[ii], csub(up, u[m])), 1.0 / a.dL);
         const double2 ey_c = make_double2(-c * df.y, c * df.x);  // (1j c) df
-        const double2 g = a.g2[b * N + m];
-        const double d = hz_dd(e[m], e[(size_t)((ii + a.nx - 1) % a.nx) * a.ny + jj]);
-        return -d * d * (g.x * ey_c.x + g.y * ey_c.y);
+        const double2 d = hz_dc(ldE(e, m), ldE(e, (size_t)((ii + a.nx - 1) % a.nx) * a.ny + jj));
+        return cscale(cmul(cmul(d, d), cmulc(a.g2[b * N + m], ey_c)), -1.0);
       };
-      acc += 0.5 * (txx(i, j) + txx(i, jp)) + 0.5 * (tyy(i, j) + tyy(ip, j));
+      acc = cadd(acc, cscale(cadd(txx(i, j), txx(i, jp)), 0.5));
+      acc = cadd(acc, cscale(cadd(tyy(i, j), tyy(ip, j)), 0.5));
     }
-    a.geps[(a.eps_shared ? 0 : (size_t)b0 * N) + n] += acc;
+    gacc((G*)a.geps, (a.eps_shared ? 0 : (size_t)b0 * N) + n, acc);
   }
 }
 
 // ------------------------------------------------------------- eps gradient
-// Ez: geps += Re(mu * x) * eps0 w^2
-// Hz: g_dyy = -(1/eps0) Re((Dxb^T mu)(Dxf x)), g_dxx likewise along y;
-//     geps += avg^T(-d^2 g_d)
+// Sensitivities c of L to d eps (geps += Re(c), or conj(c) for complex eps):
+// Ez: c = mu * x * eps0 w^2
+// Hz: c_dyy = -(1/eps0) (Dxb^T mu)(Dxf x), c_dxx likewise along y;
+//     c = avg^T(-d^2 c_d)
 struct GradArgs {
   int nx, ny, batch, eps_shared, pol;
-  const double* eps;
+  const void* eps;
   const double2* x;
   const double2* mu;
-  double* geps;
+  void* geps;
   const double2 *sfx, *sbx, *sfy, *sby;
   double2 phx, phy;
   const double* omega;
   double dL;
 };
 
+template <typename E, typename G>
 __global__ void k_grad_eps(GradArgs a) {
   const size_t N = (size_t)a.nx * a.ny;
   const int nb = a.eps_shared ? a.batch : 1;
@@ -387,19 +405,18 @@ __global__ void k_grad_eps(GradArgs a) {
   for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < N;
        n += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(n / a.ny), j = (int)(n % a.ny);
-    double acc = 0.0;
+    double2 acc = make_double2(0.0, 0.0);
     for (int bb = 0; bb < nb; ++bb) {
       const int b = b0 + bb;
       const double2* x = a.x + b * N;
       const double2* mu = a.mu + b * N;
       if (a.pol == POL_EZ) {
         const double2 p = cmul(mu[n], x[n]);
-        acc += p.x * EPSILON_0 * a.omega[b] * a.omega[b];
+        acc = cadd(acc, cscale(p, EPSILON_0 * a.omega[b] * a.omega[b]));
       } else {
-        const double* e = a.eps + (a.eps_shared ? 0 : b * N);
+        const E* e = (const E*)a.eps + (a.eps_shared ? 0 : b * N);
         const double2 *sfx = a.sfx + (size_t)b * a.nx, *sbx = a.sbx + (size_t)b * a.nx;
         const double2 *sfy = a.sfy + (size_t)b * a.ny, *sby = a.sby + (size_t)b * a.ny;
-        // g over the d_yy of cell (ii, jj)
         auto gyy = [&](int ii, int jj) {
           const size_t m = (size_t)ii * a.ny + jj;
           const int ii1 = (ii + 1) % a.nx;
@@ -410,10 +427,9 @@ __global__ void k_grad_eps(GradArgs a) {
           double2 q = cmul(sbx[ii1], mu[(size_t)ii1 * a.ny + jj]);
           if (ii == a.nx - 1) q = cmul(cconj(a.phx), q);
           const double2 dbt = csub(cmul(sbx[ii], mu[m]), q);
-          const double2 pr = cmul(dbt, dxf);
-          const double gd = -(1.0 / EPSILON_0) * pr.x / (a.dL * a.dL);
-          const double d = hz_dd(e[m], e[(size_t)((ii + a.nx - 1) % a.nx) * a.ny + jj]);
-          return -d * d * gd;
+          const double2 cd = cscale(cmul(dbt, dxf), -(1.0 / EPSILON_0) / (a.dL * a.dL));
+          const double2 d = hz_dc(ldE(e, m), ldE(e, (size_t)((ii + a.nx - 1) % a.nx) * a.ny + jj));
+          return cscale(cmul(cmul(d, d), cd), -1.0);
         };
         auto gxx = [&](int ii, int jj) {
           const size_t m = (size_t)ii * a.ny + jj;
@@ -424,16 +440,16 @@ __global__ void k_grad_eps(GradArgs a) {
           double2 q = cmul(sby[jj1], mu[(size_t)ii * a.ny + jj1]);
           if (jj == a.ny - 1) q = cmul(cconj(a.phy), q);
           const double2 dbt = csub(cmul(sby[jj], mu[m]), q);
-          const double2 pr = cmul(dbt, dyf);
-          const double gd = -(1.0 / EPSILON_0) * pr.x / (a.dL * a.dL);
-          const double d = hz_dd(e[m], e[(size_t)ii * a.ny + (jj + a.ny - 1) % a.ny]);
-          return -d * d * gd;
+          const double2 cd = cscale(cmul(dbt, dyf), -(1.0 / EPSILON_0) / (a.dL * a.dL));
+          const double2 d = hz_dc(ldE(e, m), ldE(e, (size_t)ii * a.ny + (jj + a.ny - 1) % a.ny));
+          return cscale(cmul(cmul(d, d), cd), -1.0);
         };
         const int ip = (i + 1) % a.nx, jp = (j + 1) % a.ny;
-        acc += 0.5 * (gxx(i, j) + gxx(i, jp)) + 0.5 * (gyy(i, j) + gyy(ip, j));
+        acc = cadd(acc, cscale(cadd(gxx(i, j), gxx(i, jp)), 0.5));
+        acc = cadd(acc, cscale(cadd(gyy(i, j), gyy(ip, j)), 0.5));
       }
     }
-    a.geps[(a.eps_shared ? 0 : (size_t)b0 * N) + n] += acc;
+    gacc((G*)a.geps, (a.eps_shared ? 0 : (size_t)b0 * N) + n, acc);
   }
 }
 
@@ -443,12 +459,13 @@ __global__ void k_grad_eps(GradArgs a) {
 //   Ez: +eps0 w^2 deps x
 //   Hz: -(1/eps0)(Dxb (d'yy Dxf x) + Dyb (d'xx Dyf x)),
 //       d'yy = -dyy^2 (deps + deps[i-1,j])/2, d'xx = -dxx^2 (deps + deps[i,j-1])/2
-// Restates grad_sp_solve_entries_forward (ceviche/primitives.py:139-142), whose
+// (complex products for complex eps / deps).  Restates
+// grad_sp_solve_entries_forward (ceviche/primitives.py:139-142), whose
 // sp_mult(g, indices, x) is dA.x for the entries tangent g, chained from eps.
 struct JvpArgs {
   int nx, ny, batch, eps_shared, pol;
-  const double* eps;
-  const double* deps;
+  const void* eps;
+  const void* deps;
   const double2* x;
   double2* out;
   const double2 *sfx, *sbx, *sfy, *sby;
@@ -457,12 +474,13 @@ struct JvpArgs {
   double dL;
 };
 
+template <typename E>
 __global__ void k_jvp_rhs(JvpArgs a) {
   const size_t N = (size_t)a.nx * a.ny;
   const int b = blockIdx.y;
   const size_t ebs = a.eps_shared ? 0 : N;
-  const double* e = a.eps + b * ebs;
-  const double* de = a.deps + b * ebs;
+  const E* e = (const E*)a.eps + b * ebs;
+  const E* de = (const E*)a.deps + b * ebs;
   const double2* x = a.x + b * N;
   for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < N;
        n += (size_t)gridDim.x * blockDim.x) {
@@ -470,19 +488,19 @@ __global__ void k_jvp_rhs(JvpArgs a) {
     double2 v;
     if (a.pol == POL_EZ) {
       const double w = a.omega[b];
-      v = cscale(x[n], EPSILON_0 * w * w * de[n]);
+      v = cscale(cmul(x[n], ldE(de, n)), EPSILON_0 * w * w);
     } else {
       const double2 *sfx = a.sfx + (size_t)b * a.nx, *sbx = a.sbx + (size_t)b * a.nx;
       const double2 *sfy = a.sfy + (size_t)b * a.ny, *sby = a.sby + (size_t)b * a.ny;
-      // g_x(ii) = d'yy(ii,j) (Dxf x)(ii,j) ; g_y(jj) = d'xx(i,jj) (Dyf x)(i,jj)
       auto gx = [&](int ii) {
         const size_t m = (size_t)ii * a.ny + j;
         const int ip = (ii + 1) % a.nx, im = (ii + a.nx - 1) % a.nx;
         double2 xp = x[(size_t)ip * a.ny + j];
         if (ii == a.nx - 1) xp = cmul(a.phx, xp);
         const double2 df = cscale(cmul(sfx[ii], csub(xp, x[m])), 1.0 / a.dL);
-        const double d = hz_dd(e[m], e[(size_t)im * a.ny + j]);
-        return cscale(df, -d * d * 0.5 * (de[m] + de[(size_t)im * a.ny + j]));
+        const double2 d = hz_dc(ldE(e, m), ldE(e, (size_t)im * a.ny + j));
+        const double2 dd = cscale(cmul(cmul(d, d), cadd(ldE(de, m), ldE(de, (size_t)im * a.ny + j))), -0.5);
+        return cmul(df, dd);
       };
       auto gy = [&](int jj) {
         const size_t m = (size_t)i * a.ny + jj;
@@ -490,8 +508,9 @@ __global__ void k_jvp_rhs(JvpArgs a) {
         double2 xp = x[(size_t)i * a.ny + jp];
         if (jj == a.ny - 1) xp = cmul(a.phy, xp);
         const double2 df = cscale(cmul(sfy[jj], csub(xp, x[m])), 1.0 / a.dL);
-        const double d = hz_dd(e[m], e[(size_t)i * a.ny + jm]);
-        return cscale(df, -d * d * 0.5 * (de[m] + de[(size_t)i * a.ny + jm]));
+        const double2 d = hz_dc(ldE(e, m), ldE(e, (size_t)i * a.ny + jm));
+        const double2 dd = cscale(cmul(cmul(d, d), cadd(ldE(de, m), ldE(de, (size_t)i * a.ny + jm))), -0.5);
+        return cmul(df, dd);
       };
       const int im = (i + a.nx - 1) % a.nx, jm = (j + a.ny - 1) % a.ny;
       double2 gxm = gx(im), gym = gy(jm);
@@ -507,12 +526,13 @@ __global__ void k_jvp_rhs(JvpArgs a) {
 
 // Direct eps tangent of the Hz field conversion (fdfd.py:150-162):
 // dEx += (-1j c) d'xx Dyf Hz ; dEy += (1j c) d'yy Dxf Hz, c = 1/(w eps0)
+template <typename E>
 __global__ void k_fields_jvp_hz(JvpArgs a, double2* df2) {
   const size_t N = (size_t)a.nx * a.ny;
   const int b = blockIdx.y;
   const size_t ebs = a.eps_shared ? 0 : N;
-  const double* e = a.eps + b * ebs;
-  const double* de = a.deps + b * ebs;
+  const E* e = (const E*)a.eps + b * ebs;
+  const E* de = (const E*)a.deps + b * ebs;
   const double2* u = a.x + b * N;
   const double2* sfx = a.sfx + (size_t)b * a.nx;
   const double2* sfy = a.sfy + (size_t)b * a.ny;
@@ -527,13 +547,14 @@ __global__ void k_fields_jvp_hz(JvpArgs a, double2* df2) {
     if (j == a.ny - 1) upy = cmul(a.phy, upy);
     const double2 dxf = cscale(cmul(sfx[i], csub(upx, u[n])), 1.0 / a.dL);
     const double2 dyf = cscale(cmul(sfy[j], csub(upy, u[n])), 1.0 / a.dL);
-    const double dxx = hz_dd(e[n], e[(size_t)i * a.ny + jm]);
-    const double dyy = hz_dd(e[n], e[(size_t)im * a.ny + j]);
-    const double pxx = -dxx * dxx * 0.5 * (de[n] + de[(size_t)i * a.ny + jm]);
-    const double pyy = -dyy * dyy * 0.5 * (de[n] + de[(size_t)im * a.ny + j]);
+    const double2 dxx = hz_dc(ldE(e, n), ldE(e, (size_t)i * a.ny + jm));
+    const double2 dyy = hz_dc(ldE(e, n), ldE(e, (size_t)im * a.ny + j));
+    const double2 pxx = cscale(cmul(cmul(dxx, dxx), cadd(ldE(de, n), ldE(de, (size_t)i * a.ny + jm))), -0.5);
+    const double2 pyy = cscale(cmul(cmul(dyy, dyy), cadd(ldE(de, n), ldE(de, (size_t)im * a.ny + j))), -0.5);
     // (-1j c) pxx dyf ; (1j c) pyy dxf
-    const double2 ex = make_double2(c * pxx * dyf.y, -c * pxx * dyf.x);
-    const double2 ey = make_double2(-c * pyy * dxf.y, c * pyy * dxf.x);
+    const double2 t1 = cmul(pxx, dyf), t2 = cmul(pyy, dxf);
+    const double2 ex = make_double2(c * t1.y, -c * t1.x);
+    const double2 ey = make_double2(-c * t2.y, c * t2.x);
     a.out[b * N + n] = cadd(a.out[b * N + n], ex);
     df2[b * N + n] = cadd(df2[b * N + n], ey);
   }
@@ -649,6 +670,13 @@ int cev_fdfd_plan_create(cev_fdfd_plan* out, int pol, int nx, int ny, int batch,
   return CEV_OK;
 }
 
+int cev_fdfd_plan_set_eps_complex(cev_fdfd_plan p, int on) {
+  CEV_REQUIRE(p != nullptr, "plan is NULL");
+  CEV_REQUIRE(p->mf_nsb < 0 || !on, "multi-frequency plans take a real eps");
+  p->eps_complex = on ? 1 : 0;
+  return CEV_OK;
+}
+
 int cev_fdfd_plan_destroy(cev_fdfd_plan p) {
   if (!p) return CEV_OK;
   for (int tr = 0; tr < 2; ++tr) {
@@ -676,15 +704,22 @@ int cev_fdfd_apply(cev_fdfd_plan p, const void* eps, int eps_shared, const void*
   CEV_REQUIRE(eps && x && y, "eps/x/y must be non-NULL");
   CEV_REQUIRE(x != y, "x and y must not alias");
   const int tr = transpose ? 1 : 0;
+  const bool ce = p->eps_complex != 0;
   if (precision == CEV_PREC_C128) {
+    const double os = si_units ? 1.0 / p->scale : 1.0;
+    if (ce)
+      return apply_impl<double>(p, (const double2*)eps, eps_shared, (const double2*)x,
+                                (double2*)y, tr, p->cx64[tr], p->cy64[tr], p->k2_64, os, s);
     return apply_impl<double>(p, (const double*)eps, eps_shared, (const double2*)x, (double2*)y, tr,
-                              p->cx64[tr], p->cy64[tr], p->k2_64, si_units ? 1.0 / p->scale : 1.0,
-                              s);
+                              p->cx64[tr], p->cy64[tr], p->k2_64, os, s);
   }
   CEV_REQUIRE(precision == CEV_PREC_C64, "precision must be CEV_PREC_C64 or CEV_PREC_C128");
+  const float os = si_units ? (float)(1.0 / p->scale) : 1.0f;
+  if (ce)
+    return apply_impl<float>(p, (const float2*)eps, eps_shared, (const float2*)x, (float2*)y, tr,
+                             p->cx32[tr], p->cy32[tr], p->k2_32, os, s);
   return apply_impl<float>(p, (const float*)eps, eps_shared, (const float2*)x, (float2*)y, tr,
-                           p->cx32[tr], p->cy32[tr], p->k2_32,
-                           si_units ? (float)(1.0 / p->scale) : 1.0f, s);
+                           p->cx32[tr], p->cy32[tr], p->k2_32, os, s);
 }
 
 int cev_fdfd_fields(cev_fdfd_plan p, const double* eps, int eps_shared, const void* fz, void* f1,
@@ -710,8 +745,10 @@ int cev_fdfd_fields(cev_fdfd_plan p, const double* eps, int eps_shared, const vo
   a.dL = p->dL;
   if (p->pol == CEV_POL_EZ)
     k_fields_ez<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
+  else if (p->eps_complex)
+    k_fields_hz<double2><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
   else
-    k_fields_hz<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
+    k_fields_hz<double><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
   CEV_CHECK_LAUNCH("k_fields");
   return CEV_OK;
 }
@@ -719,6 +756,7 @@ int cev_fdfd_fields(cev_fdfd_plan p, const double* eps, int eps_shared, const vo
 int cev_fdfd_fields_adjoint(cev_fdfd_plan p, const double* eps, int eps_shared, const void* fz,
                             const void* g1, const void* g2, void* gz, double* geps,
                             cudaStream_t s) {
+  const bool ce = p && p->eps_complex;
   CEV_REQUIRE(p != nullptr, "plan is NULL");
   CEV_REQUIRE(eps && g1 && g2 && gz, "NULL argument");
   FieldAdjArgs a;
@@ -743,11 +781,18 @@ int cev_fdfd_fields_adjoint(cev_fdfd_plan p, const double* eps, int eps_shared, 
   if (p->pol == CEV_POL_EZ) {
     k_fields_adj_ez<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
   } else {
-    k_fields_adj_hz<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
+    if (ce)
+      k_fields_adj_hz<double2><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
+    else
+      k_fields_adj_hz<double><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
     CEV_CHECK_LAUNCH("k_fields_adj_hz");
     if (geps) {
       CEV_REQUIRE(fz != nullptr, "Hz field adjoint with geps needs fz");
-      k_fields_adj_hz_eps<<<grid_1d(p->n(), eps_shared ? 1 : p->batch), 256, 0, s>>>(a);
+      const dim3 g = grid_1d(p->n(), eps_shared ? 1 : p->batch);
+      if (ce)
+        k_fields_adj_hz_eps<double2, double2><<<g, 256, 0, s>>>(a);
+      else
+        k_fields_adj_hz_eps<double, double><<<g, 256, 0, s>>>(a);
     }
   }
   CEV_CHECK_LAUNCH("k_fields_adj");
@@ -776,7 +821,11 @@ int cev_fdfd_grad_eps(cev_fdfd_plan p, const double* eps, int eps_shared, const 
   a.phy = p->phy;
   a.omega = p->omega_d;
   a.dL = p->dL;
-  k_grad_eps<<<grid_1d(p->n(), eps_shared ? 1 : p->batch), 256, 0, s>>>(a);
+  const dim3 g = grid_1d(p->n(), eps_shared ? 1 : p->batch);
+  if (p->eps_complex)
+    k_grad_eps<double2, double2><<<g, 256, 0, s>>>(a);
+  else
+    k_grad_eps<double, double><<<g, 256, 0, s>>>(a);
   CEV_CHECK_LAUNCH("k_grad_eps");
   return CEV_OK;
 }
@@ -788,7 +837,10 @@ int cev_fdfd_jvp_rhs(cev_fdfd_plan p, const double* eps, int eps_shared, const d
   JvpArgs a{p->nx, p->ny, p->batch, eps_shared ? 1 : 0, p->pol, eps, deps, (const double2*)x,
             (double2*)rhs, p->ft.sfx, p->ft.sbx, p->ft.sfy, p->ft.sby, p->phx, p->phy, p->omega_d,
             p->dL};
-  k_jvp_rhs<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
+  if (p->eps_complex)
+    k_jvp_rhs<double2><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
+  else
+    k_jvp_rhs<double><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a);
   CEV_CHECK_LAUNCH("k_jvp_rhs");
   return CEV_OK;
 }
@@ -801,7 +853,10 @@ int cev_fdfd_fields_jvp(cev_fdfd_plan p, const double* eps, int eps_shared, cons
   JvpArgs a{p->nx, p->ny, p->batch, eps_shared ? 1 : 0, p->pol, eps, deps, (const double2*)fz,
             (double2*)df1, p->ft.sfx, p->ft.sbx, p->ft.sfy, p->ft.sby, p->phx, p->phy, p->omega_d,
             p->dL};
-  k_fields_jvp_hz<<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a, (double2*)df2);
+  if (p->eps_complex)
+    k_fields_jvp_hz<double2><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a, (double2*)df2);
+  else
+    k_fields_jvp_hz<double><<<grid_1d(p->n(), p->batch), 256, 0, s>>>(a, (double2*)df2);
   CEV_CHECK_LAUNCH("k_fields_jvp_hz");
   return CEV_OK;
 }

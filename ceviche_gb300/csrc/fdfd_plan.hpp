@@ -34,6 +34,7 @@ struct FieldTab {
 
 struct cev_fdfd_plan_s {
   int pol = 0, nx = 0, ny = 0, batch = 0;
+  int eps_complex = 0;  // eps arrays are interleaved complex (lossy media)
   int npml_x = 0, npml_y = 0;
   double dL = 0, scale = 1, bloch_x = 0, bloch_y = 0;
   std::vector<double> omega;

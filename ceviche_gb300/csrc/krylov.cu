@@ -16,6 +16,7 @@
 #include <cstdlib>
 #include <cmath>
 #include <functional>
+#include <type_traits>
 #include <vector>
 
 #include "fdfd_plan.hpp"
@@ -32,10 +33,10 @@ static constexpr int DOT_GROUP = 16;
 static constexpr size_t FUSED_MAX_CELLS = (size_t)1 << 21;
 
 // --------------------------------------------------------------- residual
-template <int POL>
+template <int POL, typename E = double>
 struct ResArgs {
   int nx, ny, rows, first, m;
-  const double* eps;
+  const E* eps;
   size_t eps_bs;
   const double2* x;
   const double2* b;
@@ -48,8 +49,8 @@ struct ResArgs {
   KCtx ctx;
 };
 
-template <int POL>
-__global__ void __launch_bounds__(128) k_residual(ResArgs<POL> a) {
+template <int POL, typename E>
+__global__ void __launch_bounds__(128) k_residual(ResArgs<POL, E> a) {
   const int b = blockIdx.z;
   KState* st = a.ctx.st + b;
   if (st->done) return;
@@ -76,7 +77,8 @@ __global__ void __launch_bounds__(128) k_residual(ResArgs<POL> a) {
       r[n] = to_f(cscale(rv, inv));
       acc[0] += rv.x * rv.x + rv.y * rv.y;
     };
-    stencil_column<double, POL>(a.nx, a.ny, j, i0, i1, x, a.eps + b * a.eps_bs,
+    stencil_column<double, POL, decltype(ep), false, E>(a.nx, a.ny, j, i0, i1, x,
+                                                         a.eps + b * a.eps_bs,
                                 a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
   }
   residual_finish(acc[0], a.ctx, b, a.m, nblk, blk);
@@ -110,10 +112,10 @@ __global__ void __launch_bounds__(RED_THREADS) k_bnorm(const double2* bvec, doub
 }
 
 // ------------------------------------------------------- Arnoldi matvec
-template <int POL>
+template <int POL, typename E = float>
 struct MvArgs {
   int nx, ny, rows, m, j;
-  const float* eps;
+  const E* eps;
   size_t eps_bs;
   const float2* in;  // [B][N] with stride in_bs
   size_t in_bs;
@@ -126,8 +128,8 @@ struct MvArgs {
   KCtx ctx;
 };
 
-template <int POL>
-__global__ void __launch_bounds__(128) k_arnoldi_mv(MvArgs<POL> a) {
+template <int POL, typename E>
+__global__ void __launch_bounds__(128) k_arnoldi_mv(MvArgs<POL, E> a) {
   const int b = blockIdx.z;
   if (!a.ctx.st[b].active) return;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -139,7 +141,8 @@ __global__ void __launch_bounds__(128) k_arnoldi_mv(MvArgs<POL> a) {
   const float s = a.use_scale ? (float)a.ctx.sc[(size_t)b * (a.m + 1) + a.j] : 1.0f;
   const Coef<float> cyj = a.cy[(size_t)b * a.ny + j];
   auto ep = [&](int i, float2 v, float2) { y[(size_t)i * a.ny + j] = cscale(v, s); };
-  stencil_column<float, POL>(a.nx, a.ny, j, i0, i1, x, a.eps + b * a.eps_bs,
+  stencil_column<float, POL, decltype(ep), false, E>(a.nx, a.ny, j, i0, i1, x,
+                                                    a.eps + b * a.eps_bs,
                              a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
 }
 
@@ -486,7 +489,7 @@ static KrylovProblem stencil_problem(const cev_fdfd_plan_s* p) {
   int rows;
   launch_geometry(p->nx, p->ny, p->batch, g, bl, rows);
   P.res_blocks = (size_t)g.x * g.y;
-  P.extra_bytes = sizeof(float) * p->n() * p->batch;  // float copy of eps
+  P.extra_bytes = sizeof(float2) * p->n() * p->batch;  // float copy of (complex) eps
   return P;
 }
 
@@ -670,7 +673,8 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
   const int B = p->batch, m = o.restart;
   const int tr = o.transpose ? 1 : 0;
   float* eps32 = (float*)((char*)ws + L.extra);
-  const size_t ne = eps_shared ? N : N * B;
+  const bool ce = p->eps_complex != 0;
+  const size_t ne = (eps_shared ? N : N * B) * (ce ? 2 : 1);
   k_to_f32<<<std::min(ceil_div(ne, 256), 8u * sm_count()), 256, 0, s>>>(eps, eps32, ne);
   CEV_CHECK_LAUNCH("k_to_f32");
   dim3 sg, sb;
@@ -679,31 +683,41 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
 
   KrylovOps ops;
   ops.bscale = p->scale;
+  const size_t ebs = eps_shared ? 0 : N;
   ops.residual = [&](const KCtx& c, float2* V0, cudaStream_t st) -> int {
+    auto go = [&](auto pol_tag, auto e_tag) {
+      constexpr int POL = decltype(pol_tag)::value;
+      using E = decltype(e_tag);
+      ResArgs<POL, E> a{p->nx, p->ny, rows, 0, m, (const E*)eps, ebs, (const double2*)xvec,
+                        (const double2*)bvec, p->scale, p->cx64[tr], p->cy64[tr], p->k2_64, V0, N,
+                        c};
+      k_residual<POL, E><<<sg, sb, 0, st>>>(a);
+    };
     if (p->pol == POL_EZ) {
-      ResArgs<POL_EZ> a{p->nx, p->ny, rows, 0, m, eps, eps_shared ? 0 : N, (const double2*)xvec,
-                        (const double2*)bvec, p->scale, p->cx64[tr], p->cy64[tr], p->k2_64, V0, N,
-                        c};
-      k_residual<POL_EZ><<<sg, sb, 0, st>>>(a);
+      if (ce) go(std::integral_constant<int, POL_EZ>{}, double2{});
+      else go(std::integral_constant<int, POL_EZ>{}, double{});
     } else {
-      ResArgs<POL_HZ> a{p->nx, p->ny, rows, 0, m, eps, eps_shared ? 0 : N, (const double2*)xvec,
-                        (const double2*)bvec, p->scale, p->cx64[tr], p->cy64[tr], p->k2_64, V0, N,
-                        c};
-      k_residual<POL_HZ><<<sg, sb, 0, st>>>(a);
+      if (ce) go(std::integral_constant<int, POL_HZ>{}, double2{});
+      else go(std::integral_constant<int, POL_HZ>{}, double{});
     }
     CEV_CHECK_LAUNCH("k_residual");
     return CEV_OK;
   };
   ops.matvec = [&](const KCtx& c, int j, const float2* in, int use_scale, float2* out,
                    cudaStream_t st) -> int {
+    auto go = [&](auto pol_tag, auto e_tag) {
+      constexpr int POL = decltype(pol_tag)::value;
+      using E = decltype(e_tag);
+      MvArgs<POL, E> a{p->nx, p->ny, rows, m, j, (const E*)eps32, ebs, in, N, use_scale,
+                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
+      k_arnoldi_mv<POL, E><<<sg, sb, 0, st>>>(a);
+    };
     if (p->pol == POL_EZ) {
-      MvArgs<POL_EZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, N, use_scale,
-                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
-      k_arnoldi_mv<POL_EZ><<<sg, sb, 0, st>>>(a);
+      if (ce) go(std::integral_constant<int, POL_EZ>{}, float2{});
+      else go(std::integral_constant<int, POL_EZ>{}, float{});
     } else {
-      MvArgs<POL_HZ> a{p->nx, p->ny, rows, m, j, eps32, eps_shared ? 0 : N, in, N, use_scale,
-                       out, N, p->cx32[tr], p->cy32[tr], p->k2_32, c};
-      k_arnoldi_mv<POL_HZ><<<sg, sb, 0, st>>>(a);
+      if (ce) go(std::integral_constant<int, POL_HZ>{}, float2{});
+      else go(std::integral_constant<int, POL_HZ>{}, float{});
     }
     CEV_CHECK_LAUNCH("k_arnoldi_mv");
     return CEV_OK;
@@ -716,13 +730,13 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
   const char* benv = std::getenv("CEV_FUSED_BLOCKS");
   if (!(fenv && fenv[0] == '0') && B <= FUSED_MAX_BATCH && o.precond == CEV_PRECOND_NONE &&
       N * B <= FUSED_MAX_CELLS)
-    cyc_blocks = cycle_plan(p->nx, p->ny, p->pol, B, benv ? std::atoi(benv) : 0, cyc_rows,
-                            cyc_tiles, cyc_units, cyc_gp);
+    cyc_blocks = cycle_plan(p->nx, p->ny, p->pol, ce ? 1 : 0, B, benv ? std::atoi(benv) : 0,
+                            cyc_rows, cyc_tiles, cyc_units, cyc_gp);
   if (cyc_blocks > 0) {
     ops.cycle = [&](const KCtx& c, float2* V, cudaStream_t st) -> int {
       CycArgs a{p->nx, p->ny, cyc_rows, m, o.reorth, cyc_tiles, cyc_units, B, cyc_gp, N,
-                eps_shared ? 0 : N, eps32, p->cx32[tr], p->cy32[tr], p->k2_32, V, c};
-      return cycle_launch(p->pol, cyc_blocks, a, st);
+                ebs, eps32, p->cx32[tr], p->cy32[tr], p->k2_32, V, c};
+      return cycle_launch(p->pol, ce ? 1 : 0, cyc_blocks, a, st);
     };
   }
   Precond pc;

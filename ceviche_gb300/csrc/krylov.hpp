@@ -79,8 +79,8 @@ struct CycArgs {
   int nx, ny, rows, m, reorth, tiles_y, units;
   int B, gp;      // problems, blocks per problem
   size_t N;
-  size_t eps_bs;  // eps batch stride (0: shared)
-  const float* eps;
+  size_t eps_bs;    // eps batch stride in elements (0: shared)
+  const void* eps;  // float or float2 (complex eps)
   const Coef<float>* cx;
   const Coef<float>* cy;
   const float* k2;
@@ -91,10 +91,10 @@ int fused_max_blocks();
 size_t cycle_stage_bytes();
 // Blocks of the fused cycle for B problems on an nx x ny grid (0: not
 // available), its work split and gp blocks per problem; limit > 0 caps gp.
-int cycle_plan(int nx, int ny, int pol, int B, int limit, int& rows, int& tiles_y, int& units,
-               int& gp);
+int cycle_plan(int nx, int ny, int pol, int ceps, int B, int limit, int& rows, int& tiles_y,
+               int& units, int& gp);
 static constexpr int FUSED_MAX_BATCH = 16;
-int cycle_launch(int pol, int blocks, const CycArgs& a, cudaStream_t s);
+int cycle_launch(int pol, int ceps, int blocks, const CycArgs& a, cudaStream_t s);
 
 int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opts& o,
                const double2* b, double2* x, cev_solve_info* info, void* ws, size_t ws_bytes,

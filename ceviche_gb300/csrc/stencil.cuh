@@ -21,6 +21,8 @@
 // O(1) and the diagonal is -k^2 eps (Ez) or +k^2 (Hz), k^2 = eps0 mu0 w^2 dL^2.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace cev {
@@ -39,6 +41,24 @@ __device__ __forceinline__ R hz_d(R a, R b) {
   return R(1) / (R(0.5) * (a + b) + R(1e-5));
 }
 
+// Complex permittivity (lossy media): the same factor in complex arithmetic.
+__device__ __forceinline__ float2 hz_d(float2 a, float2 b) {
+  const float2 den = make_float2(0.5f * (a.x + b.x) + 1e-5f, 0.5f * (a.y + b.y));
+  const float q = 1.0f / (den.x * den.x + den.y * den.y);
+  return make_float2(den.x * q, -den.y * q);
+}
+__device__ __forceinline__ double2 hz_d(double2 a, double2 b) {
+  const double2 den = make_double2(0.5 * (a.x + b.x) + 1e-5, 0.5 * (a.y + b.y));
+  const double q = 1.0 / (den.x * den.x + den.y * den.y);
+  return make_double2(den.x * q, -den.y * q);
+}
+
+// v * e for a real or complex permittivity-derived factor e
+template <typename C, typename R>
+__device__ __forceinline__ C emul(C v, R e) { return cscale(v, e); }
+__device__ __forceinline__ float2 emul(float2 v, float2 e) { return cmul(v, e); }
+__device__ __forceinline__ double2 emul(double2 v, double2 e) { return cmul(v, e); }
+
 // Loads of the stencil input: the read-only path (the input is not written
 // during the launch), or with CG = true through L2 only (ld.global.cg), for
 // kernels that read vectors other blocks wrote earlier in the same launch.
@@ -52,11 +72,12 @@ __device__ __forceinline__ T ldx(const T* p) {
 
 // Sliding-window row iterator over one column j for rows [i0, i1).
 // Calls ep(i, Au, u_c) for every row with Au the stencil (without output
-// scaling) and u_c the centre value.
-template <typename R, int POL, typename Epi, bool CG = false>
+// scaling) and u_c the centre value.  E is the permittivity element: R (real
+// eps) or Cplx<R> (complex eps, lossy media).
+template <typename R, int POL, typename Epi, bool CG = false, typename E = R>
 __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, int i1,
                                                const Cplx<R>* x,
-                                               const R* __restrict__ eps,
+                                               const E* __restrict__ eps,
                                                const Coef<R>* __restrict__ cx,
                                                const Coef<R>& cyj, R k2, Epi& ep) {
   using C = Cplx<R>;
@@ -67,11 +88,11 @@ __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, in
   C u_m = ldx<CG>(x + (size_t)im0 * ny + j);
   C u_c = ldx<CG>(x + (size_t)i0 * ny + j);
   // Hz: eps window along i (for d_yy) ; Ez: unused
-  R e_m = R(0), dyy_m = R(0);
+  E e_m{}, dyy_m{};
   if (POL == POL_HZ) {
     const int imm = (im0 == 0) ? nx - 1 : im0 - 1;
     e_m = eps[(size_t)im0 * ny + j];
-    dyy_m = hz_d<R>(e_m, eps[(size_t)imm * ny + j]);
+    dyy_m = hz_d(e_m, eps[(size_t)imm * ny + j]);
   }
   const C ym_c = cyj.cm, yp_c = cyj.cp, ym_a = cyj.am, yp_a = cyj.ap;
   for (int i = i0; i < i1; ++i) {
@@ -83,7 +104,7 @@ __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, in
     const Coef<R> c = cx[i];
     C acc;
     if (POL == POL_EZ) {
-      const R e = eps[row + j];
+      const E e = eps[row + j];
       // x part
       C d0 = cadd(c.am, c.ap);
       d0 = cadd(d0, cadd(ym_a, yp_a));
@@ -93,22 +114,33 @@ __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, in
       acc = cfma(yp_c, u_r, acc);
       acc = csub(acc, cmul(d0, u_c));
       // A' u = -(...) - k2 eps u
-      acc.x = -acc.x - k2 * e * u_c.x;
-      acc.y = -acc.y - k2 * e * u_c.y;
+      if constexpr (std::is_same<E, R>::value) {
+        acc.x = -acc.x - k2 * e * u_c.x;
+        acc.y = -acc.y - k2 * e * u_c.y;
+      } else {
+        const C eu = cmul(e, u_c);
+        acc.x = -acc.x - k2 * eu.x;
+        acc.y = -acc.y - k2 * eu.y;
+      }
     } else {
-      const R e = eps[row + j];
-      const R el = eps[row + jm];
-      const R ell = eps[row + jmm];
-      const R dyy_p = hz_d<R>(e, e_m);     // d_yy[i]   (edge i+1/2 along x)
-      const R dxx_p = hz_d<R>(e, el);      // d_xx[i,j] (edge j+1/2 along y)
-      const R dxx_m = hz_d<R>(el, ell);    // d_xx[i,j-1]
+      const E e = eps[row + j];
+      const E el = eps[row + jm];
+      const E ell = eps[row + jmm];
+      const E dyy_p = hz_d(e, e_m);     // d_yy[i]   (edge i+1/2 along x)
+      const E dxx_p = hz_d(e, el);      // d_xx[i,j] (edge j+1/2 along y)
+      const E dxx_m = hz_d(el, ell);    // d_xx[i,j-1]
       C d0;
-      d0.x = c.am.x * dyy_m + c.ap.x * dyy_p + ym_a.x * dxx_m + yp_a.x * dxx_p;
-      d0.y = c.am.y * dyy_m + c.ap.y * dyy_p + ym_a.y * dxx_m + yp_a.y * dxx_p;
-      acc = cscale(cmul(c.cm, u_m), dyy_m);
-      acc = cadd(acc, cscale(cmul(c.cp, u_p), dyy_p));
-      acc = cadd(acc, cscale(cmul(ym_c, u_l), dxx_m));
-      acc = cadd(acc, cscale(cmul(yp_c, u_r), dxx_p));
+      if constexpr (std::is_same<E, R>::value) {
+        d0.x = c.am.x * dyy_m + c.ap.x * dyy_p + ym_a.x * dxx_m + yp_a.x * dxx_p;
+        d0.y = c.am.y * dyy_m + c.ap.y * dyy_p + ym_a.y * dxx_m + yp_a.y * dxx_p;
+      } else {
+        d0 = cadd(cadd(emul(c.am, dyy_m), emul(c.ap, dyy_p)),
+                  cadd(emul(ym_a, dxx_m), emul(yp_a, dxx_p)));
+      }
+      acc = emul(cmul(c.cm, u_m), dyy_m);
+      acc = cadd(acc, emul(cmul(c.cp, u_p), dyy_p));
+      acc = cadd(acc, emul(cmul(ym_c, u_l), dxx_m));
+      acc = cadd(acc, emul(cmul(yp_c, u_r), dxx_p));
       acc = csub(acc, cmul(d0, u_c));
       acc.x += k2 * u_c.x;
       acc.y += k2 * u_c.y;

@@ -24,6 +24,12 @@ def _to_tensor(a, dtype):
     return torch.as_tensor(np.asarray(a), dtype=dtype, device="cuda")
 
 
+def _eps_tensor(eps):
+    """eps_r on the device: float64, or complex128 for a complex (lossy) eps."""
+    cplx = eps.is_complex() if torch.is_tensor(eps) else np.iscomplexobj(eps)
+    return _to_tensor(eps, torch.complex128 if cplx else torch.float64)
+
+
 class fdfd:
     """Base class (ceviche/fdfd.py:11-162)."""
 
@@ -81,18 +87,15 @@ class fdfd:
 
     def A(self, x, transpose=False):
         """Matrix-free system matrix product A x (SI units), x of grid shape."""
-        eps = _to_tensor(self.eps_r, torch.float64)
+        eps = _eps_tensor(self.eps_r)
         xt = _to_tensor(x, torch.complex128)
         y = prim.apply(self._plan(), eps, xt, transpose=transpose)
         return y.reshape(xt.shape)
 
     def solve(self, source_z):
         """Solve for the fields of this polarisation (ceviche/fdfd.py:58-76)."""
-        if np.iscomplexobj(self.eps_r) if not torch.is_tensor(self.eps_r) \
-                else self.eps_r.is_complex():
-            raise NotImplementedError("complex eps_r is not supported by the GPU solver yet")
         numpy_out = not torch.is_tensor(self.eps_r) and not torch.is_tensor(source_z)
-        eps = _to_tensor(self.eps_r, torch.float64)
+        eps = _eps_tensor(self.eps_r)
         src = source_z if torch.is_tensor(source_z) else np.asarray(source_z)
         src_dtype = torch.complex128 if (torch.is_tensor(src) and src.is_complex()) or \
             (not torch.is_tensor(src) and np.iscomplexobj(src)) else torch.float64
@@ -148,6 +151,9 @@ class fdfd_mf_ez(fdfd):
     def solve(self, source_z):
         tens = [torch.is_tensor(a) for a in (self.eps_r, self.delta, self.phi, source_z)]
         numpy_out = not any(tens)
+        if (self.eps_r.is_complex() if torch.is_tensor(self.eps_r)
+                else np.iscomplexobj(self.eps_r)):
+            raise NotImplementedError("fdfd_mf_ez takes a real eps_r")
         eps = _to_tensor(self.eps_r, torch.float64)
         delta = _to_tensor(self.delta, torch.float64)
         phi = _to_tensor(self.phi, torch.float64)

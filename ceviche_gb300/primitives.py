@@ -82,9 +82,20 @@ def get_plan(pol, shape, dL, omegas, npml, bloch=(0.0, 0.0)):
     return p
 
 
-def _eps_arg(plan, eps, dtype):
-    """eps as a contiguous (1 or batch, nx, ny) device tensor; returns (eps, shared)."""
-    e = eps.to(device=plan.device, dtype=dtype).resolve_neg().contiguous()
+_CPLX = {torch.float64: torch.complex128, torch.float32: torch.complex64}
+
+
+def _eps_arg(plan, eps, dtype, like=None):
+    """eps as a contiguous (1 or batch, nx, ny) device tensor; returns (eps, shared).
+
+    A complex eps (lossy media) is passed as interleaved complex of the
+    matching precision and switches the plan to complex eps; a tangent or
+    gradient array (``like`` = the eps it belongs to) follows that eps."""
+    cplx = (like if like is not None else eps).is_complex()
+    if like is None:
+        check(_lib.load().cev_fdfd_plan_set_eps_complex(plan.handle, int(cplx)), "set_eps_complex")
+    e = eps.to(device=plan.device, dtype=_CPLX[dtype] if cplx else dtype)
+    e = e.resolve_conj().resolve_neg().contiguous()
     if e.dim() == 2:
         e = e.unsqueeze(0)
     if e.shape[-2:] != (plan.nx, plan.ny):
@@ -222,7 +233,7 @@ def jvp_rhs(plan, eps, deps, x, rhs):
     """rhs += -(dA/d eps . deps) x (in place)."""
     lib = _lib.load()
     e, sh = _eps_arg(plan, eps, torch.float64)
-    de, _ = _eps_arg(plan, deps, torch.float64)
+    de, _ = _eps_arg(plan, deps, torch.float64, like=e)
     if de.shape != e.shape:
         de = de.expand_as(e).contiguous()
     xt = _field_arg(plan, x, torch.complex128)
@@ -234,7 +245,7 @@ def fields_jvp(plan, eps, deps, fz, df1, df2):
     """(df1, df2) += direct eps tangent of the secondary fields (Hz only)."""
     lib = _lib.load()
     e, sh = _eps_arg(plan, eps, torch.float64)
-    de, _ = _eps_arg(plan, deps, torch.float64)
+    de, _ = _eps_arg(plan, deps, torch.float64, like=e)
     if de.shape != e.shape:
         de = de.expand_as(e).contiguous()
     z = _field_arg(plan, fz, torch.complex128)

@@ -71,6 +71,18 @@ CEV_API int cev_fdfd_plan_create(cev_fdfd_plan* plan, int pol, int nx, int ny, i
                          const double* omegas, int npml_x, int npml_y, double bloch_x,
                          double bloch_y);
 CEV_API int cev_fdfd_plan_destroy(cev_fdfd_plan plan);
+
+/*
+ * Complex permittivity (lossy media; ceviche accepts a complex eps_r,
+ * fdfd.py:40-44, and its complex-eps tests run forward-mode jacobians,
+ * tests/test_gradients_fdfd_complex.py).  With on = 1 every FDFD entry point
+ * of this plan reads eps (and deps) as interleaved complex arrays of the
+ * documented precision (complex128 where double is documented, complex64 for
+ * CEV_PREC_C64 apply), and geps as complex128 accumulating the PyTorch-
+ * convention gradient dL/dRe(eps) + i dL/dIm(eps).  Default 0 (real eps).
+ * Multi-frequency plans take a real eps only.
+ */
+CEV_API int cev_fdfd_plan_set_eps_complex(cev_fdfd_plan plan, int on);
 /* Row scaling of the non-dimensional system the solver works on:
  * A' = scale*A with scale = mu0*dL^2 (Ez) or eps0*dL^2 (Hz). */
 CEV_API double cev_fdfd_plan_scale(cev_fdfd_plan plan);

@@ -153,6 +153,13 @@ def true_residual(A, x, b):
 
 
 # ---------------------------------------------------------------- gradients
+def _out(c, cplx):
+    """Gradient from the sensitivity c (dL = Re(sum c d eps)): Re(c) for a
+    real eps; conj(c) = dL/dRe + i dL/dIm (PyTorch convention) for a complex
+    (lossy) eps, for which A(eps) is holomorphic."""
+    return np.conj(c) if cplx else np.real(c)
+
+
 def grad_eps_ez(omega, dL, eps, npml, Jz, g_hx, g_hy, g_ez, source_times_eps=False,
                 bloch=(0.0, 0.0)):
     """dL/d(eps) for a real loss of (Hx, Hy, Ez) = fdfd_ez.solve(src).
@@ -176,10 +183,11 @@ def grad_eps_ez(omega, dL, eps, npml, Jz, g_hx, g_hy, g_ez, source_times_eps=Fal
     v = np.conj(g_ez.ravel()) + (-a * Dyb).T.dot(np.conj(g_hx.ravel())) \
         + (a * Dxb).T.dot(np.conj(g_hy.ravel()))
     adj = spsolve(A.T, -v)                      # primitives.py:126
-    grad = np.real(adj * x * (-EPSILON_0 * omega ** 2))   # adj[i]*x[j] on the diagonal
+    cplx = np.iscomplexobj(eps)
+    grad = _out(adj * x * (-EPSILON_0 * omega ** 2), cplx)   # adj[i]*x[j] on the diagonal
     if source_times_eps:
         # b-VJP (primitives.py:130-135): A^-T v = -adj, then b = 1j*w*eps*Jz
-        grad = grad + np.real(-adj * 1j * omega * Jz.ravel())
+        grad = grad + _out(-adj * 1j * omega * Jz.ravel(), cplx)
     return grad.reshape(shape)
 
 
@@ -206,20 +214,23 @@ def grad_eps_hz(omega, dL, eps, npml, Mz, g_ex, g_ey, g_hz, source_times_eps=Fal
     al = 1 / 1j / omega / EPSILON_0
     vex, vey, vhz = np.conj(g_ex.ravel()), np.conj(g_ey.ravel()), np.conj(g_hz.ravel())
     Dyf_x, Dxf_x = Dyf.dot(x), Dxf.dot(x)
-    # direct dependence of Ex, Ey on dxx, dyy
-    g_dxx = np.real(vex * al * Dyf_x)
-    g_dyy = np.real(vey * (-al) * Dxf_x)
+    # direct dependence of Ex, Ey on dxx, dyy (complex sensitivities; the
+    # real part is taken at the end, or the conjugate for a complex eps)
+    cplx = np.iscomplexobj(eps)
+    g_dxx = vex * al * Dyf_x
+    g_dyy = vey * (-al) * Dxf_x
     # dependence through Hz
     v = vhz + Dyf.T.dot(al * dxx * vex) + Dxf.T.dot(-al * dyy * vey)
     adj = spsolve(A.T, -v)
     # entries VJP adj[i]*x[j] for the blocks (1/eps0) Dxb diag(dyy) Dxf, etc.
-    g_dyy = g_dyy + np.real(1 / EPSILON_0 * Dxb.T.dot(adj) * Dxf_x)
-    g_dxx = g_dxx + np.real(1 / EPSILON_0 * Dyb.T.dot(adj) * Dyf_x)
+    g_dyy = g_dyy + 1 / EPSILON_0 * Dxb.T.dot(adj) * Dxf_x
+    g_dxx = g_dxx + 1 / EPSILON_0 * Dyb.T.dot(adj) * Dyf_x
     g_exx = (-dxx ** 2 * g_dxx).reshape(shape)
     g_eyy = (-dyy ** 2 * g_dyy).reshape(shape)
     grad = 0.5 * (g_exx + np.roll(g_exx, -1, axis=1)) + 0.5 * (g_eyy + np.roll(g_eyy, -1, axis=0))
+    grad = _out(grad, cplx)
     if source_times_eps:
-        grad = grad + np.real(-adj * 1j * omega * Mz.ravel()).reshape(shape)
+        grad = grad + _out(-adj * 1j * omega * Mz.ravel(), cplx).reshape(shape)
     return grad
 
 

@@ -17,6 +17,10 @@ Fixtures (all small, seeded):
                         reference objective w.r.t. eps, delta and phi
     measure.npz         utils.measure_fields time series (utils.py:316-332)
                         of Ez and Hx at three probes
+    complex_eps.npz     complex (lossy) eps: A@x, A^T@x of the Ez/Hz system
+                        matrices, solve outputs, and central differences of
+                        the objective of test_gradients_fdfd_complex.py
+                        (eps = c*eps_r, source = c*eps_r*J) in c
     modes.npz           modes.get_modes eigenvalues and eigenvectors
                         (modes.py:10-45; ARPACK phase, compare up to phase)
                         and an insert_mode source (modes.py:48-65)
@@ -190,6 +194,7 @@ def main(ref_root):
     make_mf(ceviche, utils, constants, np.random.default_rng(424242))
     make_measure(ceviche, utils, np.random.default_rng(515151))
     make_modes(ceviche, constants, np.random.default_rng(616161))
+    make_complex(ceviche, utils, np.random.default_rng(717171))
     print("fixtures written to", HERE)
 
 
@@ -297,6 +302,36 @@ def make_modes(ceviche, constants, rng):
     out["ins_epsr"] = epsr
     out["ins_src"] = modes.insert_mode(omega, 50e-9, 10, slice(5, 85), epsr, m=2)
     np.savez_compressed(os.path.join(HERE, "modes.npz"), **out)
+
+
+def make_complex(ceviche, utils, rng):
+    out = {}
+    cases = [(37, 29, [5, 4], (0.3, -0.7), 2 * np.pi * 200e12, 1e-6),
+             (30, 30, [10, 10], None, 2 * np.pi * 200e12, 1e-6)]
+    for c, (Nx, Ny, npml, bloch, omega, dL) in enumerate(cases):
+        eps = (rng.random((Nx, Ny)) + 1) + 1j * (rng.random((Nx, Ny)) + 1)
+        x = rng.standard_normal(Nx * Ny) + 1j * rng.standard_normal(Nx * Ny)
+        src = np.zeros((Nx, Ny), dtype=complex)
+        src[Nx // 2, Ny // 2] = 1e-8
+        src[Nx // 3, Ny // 4] = 0.5e-8j
+        out[f"eps{c}"], out[f"x{c}"], out[f"src{c}"] = eps, x, src
+        out[f"meta{c}"] = np.array([omega, dL, npml[0], npml[1],
+                                    *(bloch if bloch else (0.0, 0.0))])
+        for pol, cls in (("ez", ceviche.fdfd_ez), ("hz", ceviche.fdfd_hz)):
+            F = cls(omega, dL, eps, npml, bloch_phases=list(bloch) if bloch else None)
+            A = system_matrix(F, eps, utils)
+            out[f"{pol}_Ax{c}"], out[f"{pol}_ATx{c}"] = A.dot(x), A.T.dot(x)
+            out[f"{pol}_fields{c}"] = np.stack(F.solve(eps * src))
+
+            def J(cc):
+                G = cls(omega, dL, cc * eps, npml, bloch_phases=list(bloch) if bloch else None)
+                f1, f2, fz = G.solve(cc * eps * src)
+                return np.sum(np.abs(fz) ** 2 + np.abs(f1) ** 2 + np.abs(f2) ** 2)
+
+            h = 1e-6
+            out[f"{pol}_J{c}"] = np.array(J(1.0))
+            out[f"{pol}_dJdc{c}"] = np.array((J(1.0 + h) - J(1.0 - h)) / (2 * h))
+    np.savez_compressed(os.path.join(HERE, "complex_eps.npz"), **out)
 
 
 if __name__ == "__main__":

@@ -150,3 +150,56 @@ def test_modes_match_reference():
     ref = d["ins_src"]
     assert abs(abs(np.vdot(src[10, 5:85], ref[10, 5:85])) - 1) < 1e-10
     assert np.all(src[np.arange(40) != 10] == 0)
+
+
+@pytest.mark.parametrize("k", range(2))
+@pytest.mark.parametrize("pol", ["ez", "hz"])
+def test_complex_eps_operator_and_fields_match_reference(k, pol):
+    """Complex (lossy) eps: the restated system matrices and solves against
+    the reference's (fdfd.py accepts a complex eps_r)."""
+    d = _load("complex_eps.npz")
+    omega, dL, px, py, bx, by = d[f"meta{k}"]
+    eps, x, src = d[f"eps{k}"], d[f"x{k}"], d[f"src{k}"]
+    npml, bloch = [int(px), int(py)], (bx, by)
+    A = ofd.make_A(pol, omega, dL, eps, npml, bloch)
+    assert _rel(A.dot(x), d[f"{pol}_Ax{k}"]) < 1e-13
+    assert _rel(A.T.dot(x), d[f"{pol}_ATx{k}"]) < 1e-13
+    solve = ofd.solve_ez if pol == "ez" else ofd.solve_hz
+    for got, ref in zip(solve(omega, dL, eps, npml, eps * src, bloch), d[f"{pol}_fields{k}"]):
+        assert _rel(got, ref) < 1e-10
+
+
+@pytest.mark.parametrize("pol", ["ez", "hz"])
+def test_complex_eps_oracle_gradient_vs_central_differences(pol):
+    """The oracle's complex-eps gradient (conj of the holomorphic sensitivity:
+    dL/dRe + i dL/dIm) against complex central differences of the oracle
+    objective, source proportional to eps as in the reference tests."""
+    rng = np.random.default_rng(8)
+    Nx, Ny, omega, dL, npml = 14, 11, 2 * np.pi * 200e12, 1e-6, [3, 3]
+    eps = (rng.random((Nx, Ny)) + 1) + 0.05j * (rng.random((Nx, Ny)) + 1)
+    Jz = np.zeros((Nx, Ny))
+    Jz[7, 5] = 1.0
+    solve = ofd.solve_ez if pol == "ez" else ofd.solve_hz
+    gradf = ofd.grad_eps_ez if pol == "ez" else ofd.grad_eps_hz
+
+    def L(e):
+        f = solve(omega, dL, e, npml, e * Jz)
+        return sum(np.sum(np.abs(c) ** 2) for c in f)
+
+    f = solve(omega, dL, eps, npml, eps * Jz)
+    g = gradf(omega, dL, eps, npml, Jz, *[2 * c for c in f], source_times_eps=True)
+    assert np.iscomplexobj(g)
+    h = 1e-4
+    pix = [(7, 5), (8, 5), (6, 7), (9, 3)]
+    nums = []
+    for i, j in pix:
+        num = 0j
+        for unit, part in ((1.0, 1.0), (1j, 1j)):
+            ep, em = eps.copy(), eps.copy()
+            ep[i, j] += unit * h
+            em[i, j] -= unit * h
+            num += part * (L(ep) - L(em)) / (2 * h)
+        nums.append(num)
+    nums, gp = np.array(nums), np.array([g[i, j] for i, j in pix])
+    # the reference gradient tests' criterion (norm ratio, ALLOWED_RATIO 1e-4)
+    assert np.linalg.norm(nums - gp) / np.linalg.norm(nums) <= 1e-4, (nums, gp)
