@@ -19,6 +19,7 @@ import subprocess
 import sys
 import threading
 import time
+import warnings
 
 import numpy as np
 
@@ -361,6 +362,95 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def config_numbers(max_iters5=1500):
+    """The other FDFD configurations with the plain GPU Krylov path (one JSON
+    line, not part of the default run):
+      3: 600x600 adjoint gradient (forward + transposed solve + gradient kernel)
+         beside the host SuperLU forward solve of the same matrix;
+      4: 256 problems of 256x256 (binary eps, lambda 1.3-1.8 um, dL =
+         lambda0/20) solved as one batch;
+      5: 2048x2048 Ez, 16 frequencies as one batch, capped at max_iters5
+         Arnoldi iterations (plain GMRES(30) does not reach 1e-6 here): the
+         residual reached, time per iteration and the algorithmic bytes moved."""
+    import torch
+    import ceviche_gb300 as cev
+    from ceviche_gb300 import primitives as P
+    from ceviche_gb300.workloads import config3, config4_problem, config5
+    from oracle import fdfd as ofd
+    out = {}
+    # config 3
+    p = config3()
+    kw = dict(tol=1e-6, max_iters=200000, max_stall=100000)
+    F = cev.fdfd_ez(p["omega"], p["dL"], p["eps"], p["npml"], **kw)
+    probe = torch.as_tensor(p["probe"], device="cuda")
+    src = torch.as_tensor(p["src"], device="cuda")
+
+    def grad_once():
+        eps = torch.tensor(p["eps"], device="cuda", requires_grad=True)
+        F.eps_r = eps
+        _, _, ez = F.solve(src)
+        J = ((ez * probe.conj()).sum().abs() ** 2)
+        J.backward()
+        return eps.grad
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    grad_once()
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    A = ofd.make_A_ez(p["omega"], p["dL"], p["eps"], p["npml"])
+    t0 = time.perf_counter()
+    ofd.spsolve(A, 1j * p["omega"] * p["src"].ravel())
+    t_lu = time.perf_counter() - t0
+    out["config3_adjoint_gradient_600x600"] = {
+        "gpu_gradient_s": t_grad, "gpu_gradients_per_s": 1 / t_grad,
+        "cpu_spsolve_forward_s": t_lu, "cpu_cores": 1,
+        "note": "GPU: forward + transposed plain GMRES(30) solves to 1e-6 and the gradient "
+                "kernel; CPU: one SuperLU forward solve (the adjoint needs a second)"}
+    # config 4
+    probs = [config4_problem(i) for i in range(256)]
+    n4 = probs[0]["eps"].shape[0]
+    oms = np.array([q["omega"] for q in probs])
+    plan = P.get_plan("ez", (n4, n4), probs[0]["dL"], oms, probs[0]["npml"])
+    eps4 = torch.as_tensor(np.stack([q["eps"] for q in probs]))
+    b4 = torch.stack([torch.as_tensor(1j * q["omega"] * q["src"]) for q in probs])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, info = P.solve(plan, eps4, b4, tol=1e-6, max_iters=20000, max_stall=100000)
+    torch.cuda.synchronize()
+    t4 = time.perf_counter() - t0
+    conv = sum(i["code"] == 0 for i in info)
+    its = [i["iterations"] for i in info]
+    out["config4_batch256_256x256"] = {
+        "solves_per_s": len(probs) / t4, "wall_s": t4, "converged": conv, "batch": len(probs),
+        "median_iterations": float(np.median(its)), "max_iterations": int(max(its)),
+        "worst_residual": float(max(i["residual"] for i in info))}
+    # config 5
+    q = config5()
+    n5 = q["eps"].shape[0]
+    plan = P.get_plan("ez", (n5, n5), q["dL"], q["omegas"], q["npml"])
+    b5 = torch.stack([torch.as_tensor(1j * w * q["src"]) for w in q["omegas"]])
+    e5 = torch.as_tensor(q["eps"])
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, info = P.solve(plan, e5, b5, tol=1e-6, max_iters=max_iters5, max_stall=100000)
+        torch.cuda.synchronize()
+    t5 = time.perf_counter() - t0
+    it5 = max(i["iterations"] for i in info)
+    cells = n5 * n5 * len(q["omegas"])
+    out["config5_2048x2048_16omega"] = {
+        "iterations": it5, "wall_s": t5, "ms_per_iteration": 1e3 * t5 / it5,
+        "converged": sum(i["code"] == 0 for i in info),
+        "best_residual": float(min(i["residual"] for i in info)),
+        "worst_residual": float(max(i["residual"] for i in info)),
+        "algorithmic_GBps": cells * 292 * it5 / t5 / 1e9,
+        "note": "292 B/cell per GMRES(30) iteration (stencil 20 + Gram-Schmidt 16j + 24, "
+                "averaged over j = 1..30); plain Krylov does not converge here"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -368,8 +458,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-fdfd", action="store_true")
+    ap.add_argument("--configs", action="store_true",
+                    help="measure the other FDFD configurations (plain GPU Krylov) instead")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.configs:
+        print(json.dumps(config_numbers()), flush=True)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

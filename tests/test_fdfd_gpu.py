@@ -2,7 +2,7 @@
 the CPU oracle (pinned to reference fixtures) and the reference fixtures
 themselves.  Tolerances: complex128 operator 1e-13 relative; complex64
 operator 2e-6; solved fields 1e-5 relative L2 at 1e-6 FP64 residual (the
-BASELINE config-1 gate); gradients 1e-5 relative (spec target)."""
+200x200 Ez gate); gradients 1e-5 relative."""
 import os
 
 import numpy as np
@@ -91,7 +91,7 @@ def test_solve_matches_reference_fields(cev, name, pol):
 
 
 def test_config1_field_gate(cev):
-    """BASELINE config 1 (200x200 Ez): GPU field vs sparse LU <= 1e-5 rel-L2 at
+    """The 200x200 Ez workload: GPU field vs sparse LU <= 1e-5 rel-L2 at
     an FP64 true residual <= 1e-6."""
     from ceviche_gb300.workloads import config1
     p = config1()

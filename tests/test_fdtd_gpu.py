@@ -93,7 +93,7 @@ def test_blocked_runner_matches_steps(cev, precision, shape):
 
 
 def test_config2_parity(cev):
-    """BASELINE config 2: 400x400, 2000 steps, float32 GPU vs FP64 oracle,
+    """The 400x400 TM workload (2000 steps): float32 GPU vs FP64 oracle,
     rel-L2 of Ez every 100 steps."""
     from ceviche_gb300.workloads import config2
     p = config2()
