@@ -167,16 +167,36 @@ __global__ void __launch_bounds__(RED_THREADS) k_multidot(DotArgs a) {
   const size_t stride = (size_t)nblk * blockDim.x;
   for (int g0 = 0; g0 < nv; g0 += DOT_GROUP) {
     float2 acc[DOT_GROUP];
+    const float2* vp[DOT_GROUP];  // vector bases, computed once per group
 #pragma unroll
-    for (int k = 0; k < DOT_GROUP; ++k) acc[k] = make_float2(0.f, 0.f);
-    for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
-      const float2 wv = w[n];
+    for (int k = 0; k < DOT_GROUP; ++k) {
+      acc[k] = make_float2(0.f, 0.f);
+      vp[k] = a.V + ((size_t)(g0 + k) * a.B + b) * a.n;
+    }
+    if ((a.n & 1) == 0) {
+      // two cells per load (16-byte aligned: every vector starts at an even cell)
+      const float4* w4 = (const float4*)w;
+      for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < (a.n >> 1); q += stride) {
+        const float4 wv = w4[q];
 #pragma unroll
-      for (int k = 0; k < DOT_GROUP; ++k) {
-        if (g0 + k < nv) {
-          const float2 v = a.V[((size_t)(g0 + k) * a.B + b) * a.n + n];
-          acc[k].x += v.x * wv.x + v.y * wv.y;
-          acc[k].y += v.x * wv.y - v.y * wv.x;
+        for (int k = 0; k < DOT_GROUP; ++k) {
+          if (g0 + k < nv) {
+            const float4 v = ((const float4*)vp[k])[q];
+            acc[k].x += v.x * wv.x + v.y * wv.y + v.z * wv.z + v.w * wv.w;
+            acc[k].y += v.x * wv.y - v.y * wv.x + v.z * wv.w - v.w * wv.z;
+          }
+        }
+      }
+    } else {
+      for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
+        const float2 wv = w[n];
+#pragma unroll
+        for (int k = 0; k < DOT_GROUP; ++k) {
+          if (g0 + k < nv) {
+            const float2 v = vp[k][n];
+            acc[k].x += v.x * wv.x + v.y * wv.y;
+            acc[k].y += v.x * wv.y - v.y * wv.x;
+          }
         }
       }
     }
@@ -312,24 +332,53 @@ __global__ void __launch_bounds__(RED_THREADS) k_update(UpdArgs a) {
   const size_t stride = (size_t)nblk * blockDim.x;
   float nrm = 0.f;
   constexpr int G = 8;  // basis vectors loaded together (predicated) per group
-  for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
-    float2 wv = w[n];
-    for (int g0 = 0; g0 < nv; g0 += G) {
-      float2 v[G];
+  const float2* vb = a.V + (size_t)b * a.n;  // vector k at vb + k * B * n
+  const size_t vs = (size_t)a.B * a.n;
+  if ((a.n & 1) == 0) {
+    // two cells per load (16-byte aligned: every vector starts at an even cell)
+    float4* w4 = (float4*)w;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < (a.n >> 1); q += stride) {
+      float4 wv = w4[q];
+      for (int g0 = 0; g0 < nv; g0 += G) {
+        float4 v[G];
 #pragma unroll
-      for (int k = 0; k < G; ++k)
-        v[k] = (g0 + k < nv) ? a.V[((size_t)(g0 + k) * a.B + b) * a.n + n] : make_float2(0.f, 0.f);
+        for (int k = 0; k < G; ++k)
+          v[k] = (g0 + k < nv) ? ((const float4*)(vb + (size_t)(g0 + k) * vs))[q]
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-      for (int k = 0; k < G; ++k) {
-        const float2 c = u[g0 + k < nv ? g0 + k : 0];
-        if (g0 + k < nv) {
-          wv.x -= v[k].x * c.x - v[k].y * c.y;
-          wv.y -= v[k].x * c.y + v[k].y * c.x;
+        for (int k = 0; k < G; ++k) {
+          const float2 c = u[g0 + k < nv ? g0 + k : 0];
+          if (g0 + k < nv) {
+            wv.x -= v[k].x * c.x - v[k].y * c.y;
+            wv.y -= v[k].x * c.y + v[k].y * c.x;
+            wv.z -= v[k].z * c.x - v[k].w * c.y;
+            wv.w -= v[k].z * c.y + v[k].w * c.x;
+          }
         }
       }
+      w4[q] = wv;
+      nrm += wv.x * wv.x + wv.y * wv.y + wv.z * wv.z + wv.w * wv.w;
     }
-    w[n] = wv;
-    nrm += wv.x * wv.x + wv.y * wv.y;
+  } else {
+    for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
+      float2 wv = w[n];
+      for (int g0 = 0; g0 < nv; g0 += G) {
+        float2 v[G];
+#pragma unroll
+        for (int k = 0; k < G; ++k)
+          v[k] = (g0 + k < nv) ? vb[(size_t)(g0 + k) * vs + n] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+          const float2 c = u[g0 + k < nv ? g0 + k : 0];
+          if (g0 + k < nv) {
+            wv.x -= v[k].x * c.x - v[k].y * c.y;
+            wv.y -= v[k].x * c.y + v[k].y * c.x;
+          }
+        }
+      }
+      w[n] = wv;
+      nrm += wv.x * wv.x + wv.y * wv.y;
+    }
   }
   if (!a.final_pass) return;
   __shared__ double sm[32];

@@ -231,7 +231,8 @@ def test_solve_extreme_rhs_magnitudes(cev, pol, mag):
 
 @pytest.mark.parametrize("pol", ["ez", "hz"])
 @pytest.mark.parametrize("reorth", [0, 1])
-@pytest.mark.parametrize("shape,blocks", [((90, 77), None), ((61, 300), None), ((70, 40), "5")])
+@pytest.mark.parametrize("shape,blocks", [((90, 77), None), ((61, 300), None), ((70, 40), "5"),
+                                          ((45, 37), None)])
 def test_fused_cycle_matches_multikernel(cev, pol, reorth, shape, blocks, monkeypatch):
     """The single-launch restart cycle (one problem) against the per-iteration
     launch path: both reach the FP64 tolerance (1e-7), the iterates agree to
