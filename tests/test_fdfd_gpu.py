@@ -237,7 +237,8 @@ def test_fused_cycle_matches_multikernel(cev, pol, reorth, shape, blocks, monkey
     """The single-launch restart cycle (one problem) against the per-iteration
     launch path: both reach the FP64 tolerance (1e-7), the iterates agree to
     1e-5 relative and the iteration counts within 10%.  Shapes cover one and two
-    column tiles and (CEV_FUSED_BLOCKS=5) blocks looping over several units."""
+    column tiles, (CEV_FUSED_BLOCKS=5) blocks looping over several units, and an
+    odd cell count (45x37: the launch path's one-cell loads)."""
     from ceviche_gb300 import primitives as P
     rng = np.random.default_rng(17)
     Nx, Ny = shape
