@@ -133,9 +133,11 @@ void launch_geometry(int nx, int ny, int batch, dim3& grid, dim3& block, int& ro
   int bx = ny >= 128 ? 128 : ((ny + 31) / 32) * 32;
   block = dim3(bx, 1, 1);
   const int cols = (ny + bx - 1) / bx;
-  const long target = 4L * sm_count();
+  // about 64 blocks per SM: short row chunks keep many independent row
+  // loads in flight (a column sweep waits on each row's loads)
+  const long target = 64L * sm_count();
   long per = (long)cols * batch;
-  rows = (int)std::max(2L, std::min(64L, (long)nx * per / std::max(1L, target)));
+  rows = (int)std::max(2L, std::min(16L, (long)nx * per / std::max(1L, target)));
   grid = dim3(cols, (nx + rows - 1) / rows, batch);
 }
 
