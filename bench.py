@@ -407,6 +407,27 @@ def config_numbers(max_iters5=1500):
         "cpu_spsolve_forward_s": t_lu, "cpu_cores": 1,
         "note": "GPU: forward + transposed plain GMRES(30) solves to 1e-6 and the gradient "
                 "kernel; CPU: one SuperLU forward solve (the adjoint needs a second)"}
+    # config 3b: FDTD reverse-time adjoint, 400x400, 4000 steps, checkpoints every 64
+    from ceviche_gb300.workloads import config2
+    p2 = config2(steps=4000)
+    probes = [(300, 200), (200, 300), (120, 120)]
+    for rep in range(2):  # second run timed (first one builds the plan)
+        eps_t = torch.tensor(p2["eps"], device="cuda", requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        series = cev.fdtd_probe_series(eps_t, p2["dL"], p2["npml"], 4000, p2["src"], p2["amps"],
+                                       probes, precision="float32", ckpt_every=64)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        series.sum().backward()
+        torch.cuda.synchronize()
+        t_all = time.perf_counter() - t0
+    cells = p2["eps"].size * 4000
+    out["config3b_fdtd_adjoint_400x400_4000steps"] = {
+        "forward_s": t_fwd, "forward_plus_adjoint_s": t_all,
+        "forward_gcell_per_s": cells / t_fwd / 1e9,
+        "adjoint_gcell_per_s": cells / (t_all - t_fwd) / 1e9, "ckpt_every": 64,
+        "precision": "float32"}
     # config 4
     probs = [config4_problem(i) for i in range(256)]
     n4 = probs[0]["eps"].shape[0]

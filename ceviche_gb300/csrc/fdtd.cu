@@ -285,6 +285,7 @@ struct TBArgs {
   int np;
   const int* probe_idx;
   R* probe_out;   // [t][np]
+  R* dz_hist;     // HIST kernels: Dz after step t0+st goes to dz_hist[(t0+st+1)*N]
 };
 
 template <typename R, int TI, int TJ, int K, int NT>
@@ -297,7 +298,7 @@ struct Tile {
       7 * (size_t)RN * sizeof(R) + 5 * (size_t)(RI + RJ) * sizeof(R) + (size_t)K * sizeof(R);
 };
 
-template <typename R, int TI, int TJ, int K, int NT>
+template <typename R, int TI, int TJ, int K, int NT, bool HIST = false>
 __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
   using T = Tile<R, TI, TJ, K, NT>;
   constexpr int RI = T::RI, RJ = T::RJ, RN = T::RN, CPT = T::CPT;
@@ -519,6 +520,18 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
       }
     }
     __syncthreads();
+    if constexpr (HIST) {  // Dz after this step, interior cells (adjoint recompute)
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int q = tid + k * NT;
+        if (q < RN) {
+          const int r = q / RJ, c = q - r * RJ;
+          const int ii = gi0 + r, jj = gj0 + c;
+          if (r >= K && r < K + TI && c >= K && c < K + TJ && ii < a.nx && jj < a.ny)
+            a.dz_hist[(size_t)(a.t0 + st + 1) * a.nx * a.ny + (size_t)ii * a.ny + jj] = dz[k];
+        }
+      }
+    }
     // probes of interior cells: Ez after this step
     for (int k = tid; k < a.np; k += NT) {
       const int n = a.probe_idx[k];
@@ -809,12 +822,33 @@ int step_adjoint_impl(cev_fdtd_plan p, const R* dz_in, const R* dz_out, const R*
   return CEV_OK;
 }
 
+// Tile shape of the Dz-history runner (adjoint recompute): 32x48 tiles, 512
+// threads -- one extra kernel instantiation per precision.
+constexpr int HIST_CFG = 2;
+
+template <typename R>
+static int hist_launch(bool prepare, dim3 g, const TBArgs<R>& a, cudaStream_t s) {
+  constexpr TileCfg c = TILE_CFGS[HIST_CFG];
+  using T = Tile<R, c.ti, c.tj, c.k, c.nt>;
+  if (prepare) {
+    CEV_CUDA(cudaFuncSetAttribute(k_tm_tile<R, c.ti, c.tj, c.k, c.nt, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem));
+    return CEV_OK;
+  }
+  k_tm_tile<R, c.ti, c.tj, c.k, c.nt, true><<<g, c.nt, T::smem, s>>>(a);
+  return CEV_OK;
+}
+
 template <typename R>
 int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev_fdtd_io* io,
-                cudaStream_t s) {
+                cudaStream_t s, R* dz_hist = nullptr) {
   const size_t N = p->n();
   const int ns = io ? io->n_src : 0, np = io ? io->n_probe : 0;
-  const int cfg = pick_tile<R>(p->nx, p->ny);
+  int cfg = pick_tile<R>(p->nx, p->ny);
+  if (dz_hist) {  // Dz after every step: the history kernel's tile shape, if it fits
+    const TileCfg h = TILE_CFGS[HIST_CFG];
+    cfg = (p->nx >= h.ti + 2 * h.k && p->ny >= h.tj + 2 * h.k) ? HIST_CFG : -1;
+  }
   if (cfg < 0) {
     // grids smaller than one tile region: per-step kernels
     for (int t = 0; t < nsteps; ++t) {
@@ -826,6 +860,9 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
       if (np > 0)
         k_probe<R><<<(np + 127) / 128, 128, 0, s>>>((const R*)st->dz, (const R*)p->iez, np,
                                                      io->probe_idx, (R*)io->probe_out + (size_t)t * np);
+      if (dz_hist)
+        CEV_CUDA(cudaMemcpyAsync(dz_hist + (size_t)(t + 1) * N, st->dz, N * sizeof(R),
+                                 cudaMemcpyDeviceToDevice, s));
     }
     CEV_CHECK_LAUNCH("fdtd run (per step)");
     return CEV_OK;
@@ -839,11 +876,12 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
   CEV_CUDA(cudaMemcpyAsync(bufB[4], bufA[4], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   CEV_CUDA(cudaMemcpyAsync(bufB[5], bufA[5], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   static bool prepared[2][N_TILE_CFGS] = {};
+  static bool prepared_hist[2] = {};
   TBArgs<R> a{};
-  if (!prepared[sizeof(R) == 8][cfg]) {
-    int rc = tile_dispatch<R>(cfg, true, dim3(), a, s);
+  if (dz_hist ? !prepared_hist[sizeof(R) == 8] : !prepared[sizeof(R) == 8][cfg]) {
+    int rc = dz_hist ? hist_launch<R>(true, dim3(), a, s) : tile_dispatch<R>(cfg, true, dim3(), a, s);
     if (rc != CEV_OK) return rc;
-    prepared[sizeof(R) == 8][cfg] = true;
+    (dz_hist ? prepared_hist[sizeof(R) == 8] : prepared[sizeof(R) == 8][cfg]) = true;
   }
   const TileCfg tc = TILE_CFGS[cfg];
   const int K = tc.k;
@@ -867,7 +905,11 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
     a.np = np;
     a.probe_idx = np ? io->probe_idx : nullptr;
     a.probe_out = np ? (R*)io->probe_out : nullptr;
-    tile_dispatch<R>(cfg, false, g, a, s);
+    a.dz_hist = dz_hist;
+    if (dz_hist)
+      hist_launch<R>(false, g, a, s);
+    else
+      tile_dispatch<R>(cfg, false, g, a, s);
     CEV_CHECK_LAUNCH("k_tm_tile");
     std::swap(in, out);
     t += k;
@@ -894,20 +936,21 @@ int adjoint_impl(cev_fdtd_plan p, int T, int C, const cev_fdtd_io* io, const R* 
   st.hx = cur[0]; st.hy = cur[1]; st.dz = cur[2]; st.icex = cur[3]; st.icey = cur[4]; st.idz = cur[5];
   CEV_CUDA(cudaMemsetAsync(base, 0, 6 * N * sizeof(R), s));
   CEV_CUDA(cudaMemsetAsync(adj, 0, 10 * N * sizeof(R), s));
-  auto fwd_step = [&](int t) -> int {
-    int rc = step_impl<R>(p, &st, nullptr, nullptr, nullptr, 0, s);
-    if (rc != CEV_OK) return rc;
-    if (ns > 0)
-      k_add_src<R><<<(ns + 127) / 128, 128, 0, s>>>(cur[2], ns, io->src_idx, (const R*)io->src_w,
-                                                     (const R*)io->amps, t);
-    return CEV_OK;
+  // forward sweep with checkpoints of the state before steps 0, C, 2C, ...,
+  // each stretch of C steps in the time-blocked runner (sources only)
+  auto seg_io = [&](int t0) {
+    cev_fdtd_io f{};
+    f.n_src = ns;
+    f.src_idx = io->src_idx;
+    f.src_w = io->src_w;
+    f.amps = ns ? (const void*)((const R*)io->amps + t0) : nullptr;
+    return f;
   };
-  // forward sweep with checkpoints of the state before steps 0, C, 2C, ...
-  for (int t = 0; t < T; ++t) {
-    if (t % C == 0)
-      CEV_CUDA(cudaMemcpyAsync(ck + (size_t)(t / C) * 6 * N, base, 6 * N * sizeof(R),
-                               cudaMemcpyDeviceToDevice, s));
-    int rc = fwd_step(t);
+  for (int t0 = 0; t0 < T; t0 += C) {
+    CEV_CUDA(cudaMemcpyAsync(ck + (size_t)(t0 / C) * 6 * N, base, 6 * N * sizeof(R),
+                             cudaMemcpyDeviceToDevice, s));
+    const cev_fdtd_io f = seg_io(t0);
+    int rc = run_tm_impl<R>(p, &st, std::min(C, T - t0), &f, s);
     if (rc != CEV_OK) return rc;
   }
   AdjArgs<R> a;
@@ -928,11 +971,10 @@ int adjoint_impl(cev_fdtd_plan p, int T, int C, const cev_fdtd_io* io, const R* 
     CEV_CUDA(cudaMemcpyAsync(base, ck + (size_t)(seg0 / C) * 6 * N, 6 * N * sizeof(R),
                              cudaMemcpyDeviceToDevice, s));
     CEV_CUDA(cudaMemcpyAsync(seg, cur[2], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
-    for (int t = seg0; t < seg1; ++t) {
-      int rc = fwd_step(t);
+    {
+      const cev_fdtd_io f = seg_io(seg0);
+      int rc = run_tm_impl<R>(p, &st, seg1 - seg0, &f, s, seg);
       if (rc != CEV_OK) return rc;
-      CEV_CUDA(cudaMemcpyAsync(seg + (size_t)(t + 1 - seg0) * N, cur[2], N * sizeof(R),
-                               cudaMemcpyDeviceToDevice, s));
     }
     if (first) {
       // output step T (after the last step): aEz^T = w[T-1] p
