@@ -96,13 +96,21 @@ def _dist():
 
 
 def _barrier_max(value, ws):
+    """Max of a per-rank value over the replicas (the slowest rank's time)."""
     if ws == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_rate(units_per_rank, seconds_max, ws):
+    """Whole-job rate of N independent replicas: the units all ranks processed
+    divided by the slowest rank's time (weak scaling)."""
+    return units_per_rank * ws / seconds_max
 
 
 # ------------------------------------------------------------------ CPU arm
@@ -137,7 +145,8 @@ def run_reference(args):
     ws, rank, _ = _dist()
     if rank != 0:
         return
-    procs = max(1, len(os.sched_getaffinity(0)))
+    # all host cores (CEV_CPU_PROCS=<n> caps the worker processes)
+    procs = int(os.environ.get("CEV_CPU_PROCS", "0")) or max(1, len(os.sched_getaffinity(0)))
     ts = 60  # time steps per process per bench step (bounded sample)
     for _ in range(args.warmup if args.warmup < 1 else 1):
         cpu_baseline(10, 1)
@@ -296,8 +305,7 @@ def run_ours(args):
     if ws > 1:
         torch.distributed.barrier()
     total = _barrier_max(sum(times), ws)
-    cell_updates = N * steps_t * args.steps * ws
-    value = cell_updates / total / 1e9
+    value = aggregate_rate(N * steps_t * args.steps, total, ws) / 1e9
     ms_per_step = 1e3 * total / args.steps
 
     # end to end through the public API with host buffers
@@ -315,7 +323,7 @@ def run_ours(args):
             e2e_times.append(time.perf_counter() - t0)
         del G
     e2e_t = _barrier_max(float(np.median(e2e_times)), ws)
-    e2e_val = N * steps_t * ws / e2e_t / 1e9
+    e2e_val = aggregate_rate(N * steps_t, e2e_t, ws) / 1e9
 
     line = None
     if rank == 0:
