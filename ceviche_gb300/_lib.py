@@ -19,7 +19,7 @@ CEV_NOT_CONVERGED = 1
 CEV_STAGNATED = 2
 POL_EZ, POL_HZ = 0, 1
 PREC_C64, PREC_C128 = 0, 1
-PRECOND = {"none": 0, "shifted_laplacian": 1, "learned": 2}
+PRECOND = {"none": 0, "shifted_laplacian": 1, "learned": 2, "separable": 3}
 STATUS_NAMES = {0: "converged", 1: "not converged", 2: "stagnated", -1: "invalid argument",
                 -2: "CUDA error", -3: "workspace", -4: "non-finite values"}
 
@@ -28,7 +28,8 @@ class SolveOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("inner_rtol", C.c_double), ("max_iters", C.c_int),
                 ("restart", C.c_int), ("precond", C.c_int), ("transpose", C.c_int),
                 ("use_x0", C.c_int), ("reorth", C.c_int), ("max_stall", C.c_int),
-                ("mg_levels", C.c_int), ("mg_shift", C.c_double), ("learned", C.c_void_p)]
+                ("mg_levels", C.c_int), ("mg_shift", C.c_double), ("learned", C.c_void_p),
+                ("separable", C.c_void_p)]
 
 
 class SolveInfo(C.Structure):
@@ -60,6 +61,9 @@ SIGNATURES = {
     "cev_fdfd_plan_create": (I, [PP, I, I, I, I, D, C.POINTER(C.c_double), I, I, D, D]),
     "cev_fdfd_plan_destroy": (I, [P]),
     "cev_fdfd_plan_set_eps_complex": (I, [P, I]),
+    "cev_sep_precond_create": (I, [PP, P, I, P, P, P, P, P]),
+    "cev_sep_precond_destroy": (I, [P]),
+    "cev_fdfd_axis_matrix": (I, [P, I, I, I, P]),
     "cev_fdfd_plan_scale": (D, [P]),
     "cev_fdfd_apply": (I, [P, P, I, P, P, I, I, I, P]),
     "cev_solve_opts_default": (None, [C.POINTER(SolveOpts)]),

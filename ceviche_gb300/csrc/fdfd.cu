@@ -672,6 +672,27 @@ int cev_fdfd_plan_create(cev_fdfd_plan* out, int pol, int nx, int ny, int batch,
   return CEV_OK;
 }
 
+int cev_fdfd_axis_matrix(cev_fdfd_plan p, int b, int axis, int transpose, double* out) {
+  CEV_REQUIRE(p != nullptr && out != nullptr, "NULL argument");
+  CEV_REQUIRE(b >= 0 && b < p->batch, "problem %d out of range", b);
+  CEV_REQUIRE(axis == 0 || axis == 1, "axis must be 0 (x) or 1 (y)");
+  const int n = axis == 0 ? p->nx : p->ny;
+  std::vector<Coef<double>> t;
+  axis_tables(p->pol, n, axis == 0 ? p->npml_x : p->npml_y, p->dL, p->omega[b],
+              axis == 0 ? p->bloch_x : p->bloch_y, transpose != 0, t);
+  std::fill(out, out + 2 * (size_t)n * n, 0.0);
+  auto add = [&](int r, int c, double2 v) {
+    out[2 * ((size_t)r * n + c)] += v.x;
+    out[2 * ((size_t)r * n + c) + 1] += v.y;
+  };
+  for (int i = 0; i < n; ++i) {
+    add(i, (i + n - 1) % n, t[i].cm);
+    add(i, (i + 1) % n, t[i].cp);
+    add(i, i, make_double2(-(t[i].am.x + t[i].ap.x), -(t[i].am.y + t[i].ap.y)));
+  }
+  return CEV_OK;
+}
+
 int cev_fdfd_plan_set_eps_complex(cev_fdfd_plan p, int on) {
   CEV_REQUIRE(p != nullptr, "plan is NULL");
   CEV_REQUIRE(p->mf_nsb < 0 || !on, "multi-frequency plans take a real eps");

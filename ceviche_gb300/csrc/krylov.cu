@@ -672,7 +672,7 @@ int validate_opts(const cev_solve_opts& o) {
   CEV_REQUIRE(o.tol > 0 && o.tol < 1, "tol must be in (0, 1)");
   CEV_REQUIRE(o.max_iters >= 1, "max_iters must be >= 1");
   CEV_REQUIRE(o.precond == CEV_PRECOND_NONE || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN ||
-                  o.precond == CEV_PRECOND_LEARNED,
+                  o.precond == CEV_PRECOND_LEARNED || o.precond == CEV_PRECOND_SEPARABLE,
               "unknown preconditioner %d", o.precond);
   return CEV_OK;
 }
@@ -697,6 +697,7 @@ void cev_solve_opts_default(cev_solve_opts* o) {
   o->mg_levels = 0;
   o->mg_shift = 0.5;
   o->learned = nullptr;
+  o->separable = nullptr;
 }
 
 size_t cev_fdfd_solve_workspace_size(cev_fdfd_plan p, const cev_solve_opts* opts) {

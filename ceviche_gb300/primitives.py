@@ -20,7 +20,7 @@ from ._lib import check, ptr, stream_ptr
 from .constants import EPSILON_0, MU_0
 
 _DEFAULT_OPTS = dict(tol=1e-6, inner_rtol=1e-4, max_iters=20000, restart=30, precond="none",
-                     reorth=0, max_stall=20, mg_levels=0, mg_shift=0.5)
+                     reorth=0, max_stall=20, mg_levels=0, mg_shift=0.5, sep_shift=0.0)
 
 
 class SolverWarning(UserWarning):
@@ -140,7 +140,7 @@ def make_opts(**kw):
     for k, v in kw.items():
         if v is None:
             continue
-        if k not in o and k not in ("transpose", "use_x0", "learned"):
+        if k not in o and k not in ("transpose", "use_x0", "learned", "separable"):
             raise TypeError(f"unknown solver option {k!r}")
         o[k] = v
     s = _lib.SolveOpts()
@@ -158,6 +158,8 @@ def make_opts(**kw):
     s.mg_shift = float(o["mg_shift"])
     lp = o.get("learned")
     s.learned = None if lp is None else C.c_void_p(lp.handle_ptr())
+    sp = o.get("separable")
+    s.separable = None if sp is None else sp.handle
     return s
 
 
@@ -179,6 +181,11 @@ def solve(plan, eps, b, transpose=False, x0=None, strict=False, **opts):
     lib = _lib.load()
     e, sh = _eps_arg(plan, eps, torch.float64)
     bt = _field_arg(plan, b, torch.complex128)
+    keep = None
+    if opts.get("precond") == "separable" and opts.get("separable") is None:
+        keep = SeparablePrecond(plan, e, shift=opts.get("sep_shift", 0.0), transpose=transpose)
+        opts = dict(opts, separable=keep)
+        e, sh = _eps_arg(plan, eps, torch.float64)  # re-assert the eps kind on the plan
     s = make_opts(transpose=transpose, use_x0=x0 is not None, **opts)
     if x0 is not None:
         x = _field_arg(plan, x0, torch.complex128).clone()
@@ -261,6 +268,69 @@ def grad_eps(plan, eps, x, mu, geps):
     m = _field_arg(plan, mu, torch.complex128)
     check(lib.cev_fdfd_grad_eps(plan.handle, ptr(e), sh, ptr(xt), ptr(m), ptr(geps), stream_ptr()),
           "grad_eps")
+
+
+def _sep_factors(plan, transpose):
+    """Eigendecompositions of the plan's 1D axis operators (cached per plan and
+    transpose flag): device complex128 Vx, Vx^-1 [B][nx][nx], Vy, Vy^-1
+    [B][ny][ny] and the eigenvalues (complex128 [B][n])."""
+    cache = plan.__dict__.setdefault("_sep_cache", {})
+    key = bool(transpose)
+    if key in cache:
+        return cache[key]
+    lib = _lib.load()
+    out = {}
+    for axis, n, name in ((0, plan.nx, "x"), (1, plan.ny, "y")):
+        V, Vi, L = [], [], []
+        for b in range(plan.batch):
+            T = np.zeros((n, n), dtype=np.complex128)
+            check(lib.cev_fdfd_axis_matrix(plan.handle, b, axis, int(key),
+                                           T.ctypes.data_as(C.c_void_p)), "axis_matrix")
+            lam, vec = np.linalg.eig(T)
+            V.append(vec)
+            Vi.append(np.linalg.inv(vec))
+            L.append(lam)
+        dev = plan.device
+        out["v" + name] = torch.as_tensor(np.stack(V), dtype=torch.complex128, device=dev).contiguous()
+        out["vi" + name] = torch.as_tensor(np.stack(Vi), dtype=torch.complex128, device=dev).contiguous()
+        out["l" + name] = torch.as_tensor(np.stack(L), dtype=torch.complex128, device=dev)
+    cache[key] = out
+    return out
+
+
+class SeparablePrecond:
+    """CEV_PRECOND_SEPARABLE for a plan and an eps: the exact inverse of the
+    stretched operator with eps replaced by its mean c per problem (times
+    1 + i*shift), applied as dense GEMMs on the device.  The 1D
+    eigendecompositions are host LAPACK work, O(n^3) per axis and problem,
+    cached on the plan; the per-eps part is the table 1/d."""
+
+    def __init__(self, plan, eps, shift=0.0, transpose=False):
+        lib = _lib.load()
+        f = _sep_factors(plan, transpose)
+        e = eps if eps.dim() == 3 else eps.unsqueeze(0)
+        c = e.reshape(e.shape[0], -1).mean(dim=1).to(torch.complex128) * (1 + 1j * shift)
+        if c.numel() == 1 and plan.batch > 1:
+            c = c.expand(plan.batch)
+        k2 = (EPSILON_0 * MU_0 * plan.dL ** 2) * plan.omega_t ** 2
+        lam = f["lx"][:, :, None] + f["ly"][:, None, :]
+        if plan.pol_name == "ez":
+            d = -lam - (k2 * c).view(-1, 1, 1)
+        else:
+            d = lam / (c + 1e-5).view(-1, 1, 1) + k2.view(-1, 1, 1)
+        self.dinv = (1.0 / d).to(torch.complex128).contiguous()
+        self._keep = (f["vx"], f["vix"], f["vy"], f["viy"])
+        h = C.c_void_p()
+        check(lib.cev_sep_precond_create(C.byref(h), plan.handle, int(bool(transpose)),
+                                         ptr(f["vx"]), ptr(f["vix"]), ptr(f["vy"]),
+                                         ptr(f["viy"]), ptr(self.dinv)), "sep_precond_create")
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.cev_sep_precond_destroy(h)
+            self.handle = None
 
 
 class FDFDSolve(torch.autograd.Function):

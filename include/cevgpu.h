@@ -50,6 +50,7 @@ extern "C" {
 #define CEV_PRECOND_NONE 0
 #define CEV_PRECOND_SHIFTED_LAPLACIAN 1
 #define CEV_PRECOND_LEARNED 2
+#define CEV_PRECOND_SEPARABLE 3 /* exact inverse of the constant-eps stretched operator */
 
 /* Last error message of the calling thread ("" if none). */
 CEV_API const char* cev_last_error_string(void);
@@ -114,6 +115,7 @@ typedef struct {
   int mg_levels;      /* shifted-Laplacian preconditioner: multigrid levels (0 = auto) */
   double mg_shift;    /* shifted-Laplacian imaginary shift beta (default 0.5) */
   const void* learned; /* CEV_PRECOND_LEARNED: a cev_learned_precond handle */
+  const void* separable; /* CEV_PRECOND_SEPARABLE: a cev_sep_precond handle */
 } cev_solve_opts;
 
 typedef struct {
@@ -124,6 +126,39 @@ typedef struct {
   double residual; /* final FP64 true relative residual */
   double bnorm;    /* ||b|| (SI) */
 } cev_solve_info;
+
+/*
+ * Separable preconditioner (CEV_PRECOND_SEPARABLE).  With eps replaced by a
+ * constant c per problem, the stretched operator of a plan is separable:
+ *   Ez: A'_c = -(Tx (x) I + I (x) Ty) - k2 c,   Hz: A'_c = (Tx (x) I + I (x) Ty)/(c + 1e-5) + k2
+ * (k2 = eps0 mu0 w^2 dL^2; Tx, Ty the plan's 1D stencil operators, see
+ * cev_fdfd_axis_matrix).  With Tx = Vx Lx Vx^-1 and Ty = Vy Ly Vy^-1 its
+ * inverse is (Vx (x) Vy) diag(1/d) (Vx^-1 (x) Vy^-1): four dense complex
+ * GEMMs per application (cuBLAS, strided-batched over the problems) and one
+ * scaling kernel.  Used as the right preconditioner of flexible GMRES; the
+ * solve still converges on the true operator to the FP64 residual.
+ * vx, vxi: complex128 [batch][nx][nx] (row-major Vx, Vx^-1); vy, vyi:
+ * [batch][ny][ny]; dinv: complex128 [batch][nx][ny] = 1/d (complex128
+ * because the PML makes the 1D eigenbases ill-conditioned).  All device
+ * pointers, owned by the caller and kept alive with the handle.  transpose
+ * states which operator (A or A^T) the factors belong to; a solve uses the
+ * handle only with the same transpose flag.
+ */
+typedef struct cev_sep_precond_s* cev_sep_precond;
+CEV_API int cev_sep_precond_create(cev_sep_precond* out, cev_fdfd_plan plan, int transpose,
+                                   const void* vx, const void* vxi, const void* vy,
+                                   const void* vyi, const void* dinv);
+CEV_API int cev_sep_precond_destroy(cev_sep_precond h);
+
+/*
+ * The plan's 1D stencil operator along one axis (0 = x, 1 = y) for problem b
+ * and the forward (transpose = 0) or transposed tables, as a dense host
+ * matrix (n x n complex128, row-major, interleaved): row i holds cm at
+ * column i-1, cp at i+1 and -(am + ap) at i (indices mod n, Bloch phasors
+ * on the wrap), the non-dimensional derivative part of fdfd.py:172-233
+ * along that axis.  No CUDA call.
+ */
+CEV_API int cev_fdfd_axis_matrix(cev_fdfd_plan plan, int b, int axis, int transpose, double* out);
 
 /* Fills opts with the defaults documented above. */
 CEV_API void cev_solve_opts_default(cev_solve_opts* opts);
