@@ -370,6 +370,77 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def learned_numbers(train_problems=128, steps=6000, eval_batch=16, iter_cap=900):
+    """Config 4 with the learned preconditioner: build training residuals
+    with the plain solver on `train_problems` problems, train the network on
+    the GPU (Adam, physics loss through the stencil), then solve `eval_batch`
+    held-out problems with FGMRES(30)+network and with plain GMRES(30), both
+    capped at `iter_cap` iterations; plus the network's own throughput."""
+    import torch
+    from ceviche_gb300 import primitives as P
+    from ceviche_gb300.learned import LearnedPreconditioner, residual_samples
+    from ceviche_gb300.workloads import config4_problem
+
+    def group(ids):
+        pr = [config4_problem(i) for i in ids]
+        om = np.array([q["omega"] for q in pr])
+        pl = P.get_plan("ez", (256, 256), pr[0]["dL"], om, pr[0]["npml"])
+        ep = torch.as_tensor(np.stack([q["eps"] for q in pr])).cuda()
+        bb = torch.stack([torch.as_tensor(1j * q["omega"] * q["src"]) for q in pr]).cuda()
+        return pl, ep, bb
+
+    iters = (0, 10, 30, 90, 270, 810)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    samples = []
+    for g0 in range(0, train_problems, 16):
+        pl, ep, bb = group(range(g0, g0 + 16))
+        samples += [(pl, ep, r) for r in residual_samples(pl, ep, bb, iters=iters)]
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    net = LearnedPreconditioner(256, 256, max_batch=16, c0=32, seed=0)
+    t0 = time.perf_counter()
+    net.fit(samples, steps=steps, lr=5e-4)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    pl, ep, bb = group(range(256, 256 + eval_batch))
+    held = [float(net.loss_and_grad(pl, ep, r)[0]) for r in residual_samples(pl, ep, bb, iters=iters)]
+    res = {}
+    for name, kw in (("plain", {}), ("learned", dict(precond="learned", learned=net))):
+        for k in (30, 90, 300, iter_cap):
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                _, info = P.solve(pl, ep, bb, tol=1e-6, max_iters=k, max_stall=10 ** 6, **kw)
+                torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            res[f"{name}_at_{k}"] = {
+                "median_residual": float(np.median([i["residual"] for i in info])),
+                "converged": int(sum(i["code"] == 0 for i in info)), "wall_s": dt,
+                "ms_per_iteration": 1e3 * dt / k}
+    # network throughput: forward on a 16-problem batch
+    r = bb.to(torch.complex64)
+    for _ in range(3):
+        net.forward(pl, ep, r)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(20):
+        net.forward(pl, ep, r)
+    torch.cuda.synchronize()
+    tf = (time.perf_counter() - t0) / 20
+    c = 32
+    macs_px = (8 * c + 2 * c * c / 4 + 8 * c * c / 16 + (32 + 64 + 32) * c * c / 64
+               + (16 + 8) * c * c / 16 + (4 + 2) * c * c / 4 + c * c) * 9
+    flops = 2 * macs_px * eval_batch * 256 * 256
+    return {"train_problems": train_problems, "train_steps": steps, "data_s": t_data,
+            "train_s": t_train, "heldout_loss_by_plain_iterate": dict(zip(map(str, iters), held)),
+            "eval_batch": eval_batch, "solves": res,
+            "network_forward_ms_batch16": 1e3 * tf, "network_forward_tflops": flops / tf / 1e12,
+            "note": "tol 1e-6 FP64 true residual; neither method reaches it within the cap; "
+                    "median residual at equal iteration counts is the comparison"}
+
+
 def config_numbers(max_iters5=1500):
     """The other FDFD configurations with the plain GPU Krylov path (one JSON
     line, not part of the default run):
@@ -454,6 +525,7 @@ def config_numbers(max_iters5=1500):
         "solves_per_s": len(probs) / t4, "wall_s": t4, "converged": conv, "batch": len(probs),
         "median_iterations": float(np.median(its)), "max_iterations": int(max(its)),
         "worst_residual": float(max(i["residual"] for i in info))}
+    out["config4_learned_vs_plain_256x256"] = learned_numbers()
     # config 5
     q = config5()
     n5 = q["eps"].shape[0]

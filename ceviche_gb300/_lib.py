@@ -63,6 +63,13 @@ SIGNATURES = {
     "cev_fdfd_plan_set_eps_complex": (I, [P, I]),
     "cev_sep_precond_create": (I, [PP, P, I, P, P, P, P, P]),
     "cev_sep_precond_destroy": (I, [P]),
+    "cev_learned_param_count": (I, [I, C.POINTER(S)]),
+    "cev_learned_create": (I, [PP, I, I, I, I]),
+    "cev_learned_set_params": (I, [P, P, P]),
+    "cev_learned_forward": (I, [P, P, P, I, P, P, P]),
+    "cev_learned_backward": (I, [P, P, P, P]),
+    "cev_adam_step": (I, [P, P, P, P, S, C.c_float, C.c_float, C.c_float, C.c_float, I, P]),
+    "cev_learned_destroy": (I, [P]),
     "cev_fdfd_axis_matrix": (I, [P, I, I, I, P]),
     "cev_fdfd_plan_scale": (D, [P]),
     "cev_fdfd_apply": (I, [P, P, I, P, P, I, I, I, P]),

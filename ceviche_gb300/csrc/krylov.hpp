@@ -113,4 +113,11 @@ int precond_setup(Precond& pc, const cev_fdfd_plan_s* p, const cev_solve_opts& o
 int precond_apply(Precond& pc, const KCtx& c, int j, int m, const float2* v, float2* z,
                   cudaStream_t s);
 
+namespace nn {
+int learned_check(const cev_learned_precond_s* h, const cev_fdfd_plan_s* p);
+int learned_forward(cev_learned_precond_s* h, const cev_fdfd_plan_s* p, const float* eps,
+                    int eps_shared, const float2* r, float2* z, const double* sc, int sc_stride,
+                    int sc_index, cudaStream_t s);
+}  // namespace nn
+
 }  // namespace cev

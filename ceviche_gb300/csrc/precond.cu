@@ -44,10 +44,27 @@ struct SepState {
   int B = 0, m = 0;
 };
 
-int precond_setup(Precond& pc, const cev_fdfd_plan_s* p, const cev_solve_opts& o, const float*,
-                  int, void* ws, cudaStream_t) {
+// CEV_PRECOND_LEARNED: the network of csrc/learned.cu, z = sc_j * f(v_j)
+struct LearnedState {
+  cev_learned_precond_s* h;
+  const cev_fdfd_plan_s* p;
+  const float* eps;
+  int eps_shared;
+};
+
+int precond_setup(Precond& pc, const cev_fdfd_plan_s* p, const cev_solve_opts& o, const float* eps32,
+                  int eps_shared, void* ws, cudaStream_t) {
   pc.kind = o.precond;
   if (o.precond == CEV_PRECOND_NONE) return CEV_OK;
+  if (o.precond == CEV_PRECOND_LEARNED) {
+    auto* h = (cev_learned_precond_s*)o.learned;
+    const int rc = nn::learned_check(h, p);
+    if (rc != CEV_OK) return rc;
+    static thread_local LearnedState ls;  // one Precond per solve call, as above
+    ls = LearnedState{h, p, eps32, eps_shared};
+    pc.impl = &ls;
+    return CEV_OK;
+  }
   CEV_REQUIRE(o.precond == CEV_PRECOND_SEPARABLE, "preconditioner %d is not available", o.precond);
   auto* h = (cev_sep_precond_s*)o.separable;
   CEV_REQUIRE(h != nullptr, "CEV_PRECOND_SEPARABLE needs opts.separable");
@@ -94,7 +111,12 @@ __global__ void k_c128_to_c64(const double2* __restrict__ in, float2* __restrict
 
 int precond_apply(Precond& pc, const KCtx& c, int j, int m, const float2* v, float2* z,
                   cudaStream_t s) {
-  CEV_REQUIRE(pc.kind == CEV_PRECOND_SEPARABLE && pc.impl, "no preconditioner configured");
+  CEV_REQUIRE(pc.impl != nullptr, "no preconditioner configured");
+  if (pc.kind == CEV_PRECOND_LEARNED) {
+    const LearnedState& ls = *(const LearnedState*)pc.impl;
+    return nn::learned_forward(ls.h, ls.p, ls.eps, ls.eps_shared, v, z, c.sc, m + 1, j, s);
+  }
+  CEV_REQUIRE(pc.kind == CEV_PRECOND_SEPARABLE, "no preconditioner configured");
   SepState& st = *(SepState*)pc.impl;
   cev_sep_precond_s& h = *st.h;
   const int nx = h.nx, ny = h.ny, B = h.batch;

@@ -151,6 +151,38 @@ CEV_API int cev_sep_precond_create(cev_sep_precond* out, cev_fdfd_plan plan, int
 CEV_API int cev_sep_precond_destroy(cev_sep_precond h);
 
 /*
+ * Learned preconditioner (CEV_PRECOND_LEARNED).  A 4-level convolutional
+ * encoder-decoder (base width c0: c0 -> 8*c0 channels, bf16 activations,
+ * fp32 accumulation on the tensor cores) that maps a Krylov basis vector of a
+ * single-frequency Ez plan to an approximation of A'^-1 v.  It has no
+ * counterpart in ceviche: it is the right preconditioner of the flexible
+ * GMRES that replaces ceviche's direct solve (ceviche/solvers.py:37-62).
+ *
+ * Parameters are one fp32 device vector of cev_learned_param_count(c0)
+ * numbers: per conv layer W[cout][cin][3][3] then b[cout], then the 1x1
+ * head W[2][c0], b[2].  The caller owns parameters, gradients and the Adam
+ * state; the handle owns the packed bf16 weights and the activations for
+ * max_batch problems of nx x ny (both divisible by 8).
+ *
+ * forward: z = |r| f(r/|r|, eps, k2) for every problem of the plan (r, z
+ *   complex64 [batch][nx][ny]; eps float [batch][nx][ny] or shared).
+ * backward: grad += dL/dparams for dL/dz = gz (complex64, d/dRe + i d/dIm),
+ *   through the activations of the last forward.
+ * cev_adam_step: one Adam update of n parameters (step counts from 1).
+ */
+typedef struct cev_learned_precond_s* cev_learned_precond;
+CEV_API int cev_learned_param_count(int c0, size_t* count);
+CEV_API int cev_learned_create(cev_learned_precond* out, int nx, int ny, int max_batch, int c0);
+CEV_API int cev_learned_set_params(cev_learned_precond h, const float* params, cudaStream_t stream);
+CEV_API int cev_learned_forward(cev_learned_precond h, cev_fdfd_plan plan, const float* eps,
+                                int eps_shared, const void* r, void* z, cudaStream_t stream);
+CEV_API int cev_learned_backward(cev_learned_precond h, const void* gz, float* grad,
+                                 cudaStream_t stream);
+CEV_API int cev_adam_step(float* p, const float* g, float* m, float* v, size_t n, float lr,
+                          float beta1, float beta2, float eps, int step, cudaStream_t stream);
+CEV_API int cev_learned_destroy(cev_learned_precond h);
+
+/*
  * The plan's 1D stencil operator along one axis (0 = x, 1 = y) for problem b
  * and the forward (transpose = 0) or transposed tables, as a dense host
  * matrix (n x n complex128, row-major, interleaved): row i holds cm at
