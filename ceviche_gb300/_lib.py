@@ -69,6 +69,8 @@ SIGNATURES = {
     "cev_learned_forward": (I, [P, P, P, I, P, P, P]),
     "cev_learned_backward": (I, [P, P, P, P]),
     "cev_adam_step": (I, [P, P, P, P, S, C.c_float, C.c_float, C.c_float, C.c_float, I, P]),
+    "cev_learned_set_conv_impl": (I, [I]),
+    "cev_learned_tc_fault": (I, [C.POINTER(I)]),
     "cev_learned_destroy": (I, [P]),
     "cev_fdfd_axis_matrix": (I, [P, I, I, I, P]),
     "cev_fdfd_plan_scale": (D, [P]),

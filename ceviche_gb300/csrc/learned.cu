@@ -458,23 +458,36 @@ __global__ void __launch_bounds__(256) k_bias_grad(const bf16* __restrict__ g, f
   }
 }
 
-// per-problem RMS of r: nrm[b] = sqrt(mean |r|^2)
-__global__ void __launch_bounds__(512) k_rms(const float2* __restrict__ r, size_t n, float* nrm) {
-  const int b = blockIdx.x;
+// per-problem RMS of r: nrm[b] = sqrt(mean |r|^2), two passes: RMS_PARTS
+// blocks per problem write partial sums, then one thread per problem adds them
+constexpr int RMS_PARTS = 32;
+
+__global__ void __launch_bounds__(256) k_rms_part(const float2* __restrict__ r, size_t n,
+                                                  double* __restrict__ part) {
+  const int b = blockIdx.y;
   const float2* rb = r + (size_t)b * n;
   double acc = 0.0;
-  for (size_t e = threadIdx.x; e < n; e += blockDim.x) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+       e += (size_t)gridDim.x * blockDim.x) {
     const float2 v = rb[e];
     acc += (double)v.x * v.x + (double)v.y * v.y;
   }
-  __shared__ double s[512];
+  __shared__ double s[256];
   s[threadIdx.x] = acc;
   __syncthreads();
-  for (int w = 256; w > 0; w >>= 1) {
+  for (int w = 128; w > 0; w >>= 1) {
     if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) nrm[b] = (float)sqrt(s[0] / (double)n);
+  if (threadIdx.x == 0) part[(size_t)b * RMS_PARTS + blockIdx.x] = s[0];
+}
+
+__global__ void k_rms_final(const double* __restrict__ part, size_t n, int B, float* nrm) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  double t = 0.0;
+  for (int k = 0; k < RMS_PARTS; ++k) t += part[(size_t)b * RMS_PARTS + k];
+  nrm[b] = (float)sqrt(t / (double)n);
 }
 
 // input features, bf16 [npix][8]
@@ -621,6 +634,248 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
   }
 }
 
+// ------------------------------------------------ 3x3 conv on tcgen05 (TMEM accumulators)
+// The conv as an implicit GEMM on the 5th-generation tensor cores.  A CTA
+// owns a 16 x 8 pixel tile (M = 128) and BN output channels; one thread
+// issues tcgen05.mma (K = 16 per instruction) from shared-memory
+// descriptors and the fp32 accumulator tile lives in TMEM (BN columns x 128
+// lanes), read back by tcgen05.ld for the fused bias/ReLU epilogue.
+//
+// Operand layout: K-major, no swizzle, core matrices of 8 rows x 16 B.
+//  * A: for each 32-channel slab the 18 x 10 halo tile of the input is
+//    staged once as 180 pixel lines of 16 B (8 channels) per 8-channel chunk.
+//    An output row of the tile is one 8-row core-matrix group, so the
+//    stride-dimension offset is one halo row (160 B) and the leading-
+//    dimension offset one channel chunk (2880 B).  Tap (dy, dx) is the same
+//    descriptor with its start moved by ((1+dy)*10 + 1+dx) lines: the 9 taps
+//    reuse one staged tile instead of nine.
+//  * B: the slab's weights for all 9 taps, [tap][BN rows][32 channels] as
+//    core matrices (leading offset 128 B, stride offset 512 B).
+// Two slabs are in flight when the layer has more than one; an mbarrier per
+// stage, armed by tcgen05.commit, tells the loaders when the MMAs reading a
+// stage are done.  Every wait is bounded: on timeout the kernel records the
+// fault, waits (bounded) for its own MMAs, frees TMEM and returns.
+
+constexpr int HX_TI = 16, HX_TJ = 8;                 // output tile (rows i, columns j)
+constexpr int HX_HJ = HX_TJ + 2;                     // halo width
+constexpr int HX_LINES = (HX_TI + 2) * HX_HJ;        // 180 pixel lines per channel chunk
+constexpr int HX_LBO = HX_LINES * 16;                // 2880 B between 8-channel chunks
+constexpr int HX_SBO = HX_HJ * 16;                   // 160 B between output rows
+constexpr int HX_SLAB_A = (CBK / 8) * HX_LBO;        // 11520 B per 32-channel slab
+constexpr long long TC_SPIN = 1LL << 22;
+
+__device__ int g_tc_fault = 0;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned addr, unsigned parity) {
+  for (long long i = 0; i < TC_SPIN; ++i) {
+    unsigned ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle
+__device__ __forceinline__ unsigned long long tc_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
+  return (unsigned long long)((saddr >> 4) & 0x3FFFu) |
+         ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ULL << 46);
+}
+
+template <int BN> struct TcGeom {
+  static constexpr int TAP_B = BN * CBK * 2;       // one tap's weights: BN x 32 channels
+  static constexpr int SLAB = HX_SLAB_A + 9 * TAP_B;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ unsigned tslot;
+  constexpr int SLAB = TcGeom<BN>::SLAB, TAP_B = TcGeom<BN>::TAP_B;
+  // instruction descriptor: f32 accumulate, bf16 A and B, both K-major, N = BN, M = 128
+  constexpr unsigned IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(BN >> 3) << 17) |
+                             ((unsigned)(CBM >> 4) << 24);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_j = (a.W + HX_TJ - 1) / HX_TJ, tiles_i = (a.H + HX_TI - 1) / HX_TI;
+  int t = blockIdx.x;
+  const int tj = t % tiles_j;
+  t /= tiles_j;
+  const int ti = t % tiles_i;
+  const int b = t / tiles_i;
+  const int i0 = ti * HX_TI, j0 = tj * HX_TJ;
+  const int n0 = blockIdx.y * BN;
+  const long long img = (long long)b * a.H * a.W;
+  const int nslab = a.cinp / CBK;
+  const unsigned sbase = smem_u32(tc_smem);
+  if (tid == 0) {
+    for (int q = 0; q < 2; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[q])));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(&tslot)),
+                 "r"(BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const unsigned tmem = tslot;
+
+  auto load = [&](int sl, int st) {
+    unsigned char* sa = tc_smem + (size_t)st * SLAB;
+    unsigned char* sb = sa + HX_SLAB_A;
+    const int c0 = sl * CBK;
+    for (int e = tid; e < (CBK / 8) * HX_LINES; e += 128) {
+      const int c = e / HX_LINES, L = e - c * HX_LINES;
+      const int hr = L / HX_HJ, hc = L - hr * HX_HJ;
+      const int i = i0 - 1 + hr, j = j0 - 1 + hc, ch = c0 + c * 8;
+      const bool v = i >= 0 && i < a.H && j >= 0 && j < a.W && ch < a.cin;
+      const void* src =
+          v ? (const void*)(a.in + (img + (long long)i * a.W + j) * a.in_cs + ch) : (const void*)a.in;
+      cp_async16(sa + c * HX_LBO + L * 16, src, v);
+    }
+    for (int e = tid; e < 9 * BN * (CBK / 8); e += 128) {
+      const int c = e & 3, rt = e >> 2;
+      const int row = rt % BN, tap = rt / BN;
+      const int co = n0 + row;
+      const bool v = co < a.cout;
+      const void* src =
+          v ? (const void*)(a.w + ((size_t)tap * a.cout + co) * a.cinp + c0 + c * 8) : (const void*)a.w;
+      cp_async16(sb + tap * TAP_B + (row >> 3) * 512 + (row & 7) * 16 + c * 128, src, v);
+    }
+    cp_commit();
+  };
+
+  bool ok = true;
+  int issued = -1;
+  load(0, 0);
+  for (int sl = 0; sl < nslab && ok; ++sl) {
+    const int st = sl & 1;
+    cp_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const unsigned sa = sbase + (unsigned)(st * SLAB), sb = sa + HX_SLAB_A;
+#pragma unroll
+      for (int tap = 0; tap < 9; ++tap) {
+        const unsigned aoff = (unsigned)(((tap / 3) * HX_HJ + (tap % 3)) * 16);
+#pragma unroll
+        for (int kk = 0; kk < CBK / 16; ++kk) {
+          const unsigned long long ad = tc_desc(sa + kk * 2 * HX_LBO + aoff, HX_LBO, HX_SBO);
+          const unsigned long long bd = tc_desc(sb + tap * TAP_B + kk * 256, 128, 512);
+          const unsigned acc = (sl > 0 || tap > 0 || kk > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+              "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_u32(&mbar[st]))
+                   : "memory");
+    }
+    issued = sl;
+    if (sl + 1 < nslab) {
+      // stage (sl + 1) & 1 was last read by the MMAs of slab sl - 1
+      bool w = true;
+      if (sl >= 1) w = mbar_wait(smem_u32(&mbar[(sl - 1) & 1]), (unsigned)(((sl - 1) >> 1) & 1));
+      ok = __syncthreads_and(w ? 1 : 0) != 0;  // block-uniform, so the loop exits together
+      if (ok) load(sl + 1, (sl + 1) & 1);
+    }
+  }
+  // the last commit covers every earlier tcgen05.mma of the issuing thread
+  if (issued >= 0) {
+    const bool done = mbar_wait(smem_u32(&mbar[issued & 1]), (unsigned)((issued >> 1) & 1));
+    ok = ok && done;
+  }
+  cp_wait_all();
+  if (!ok) atomicExch(&g_tc_fault, 1);
+  const int all_ok = __syncthreads_and(ok ? 1 : 0);
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  if (all_ok) {
+    // TMEM lane m = 8 * (tile row) + (tile column); warp w owns lanes 32w..32w+31
+    const int m = warp * 32 + lane;
+    const int i = i0 + m / HX_TJ, j = j0 + m % HX_TJ;
+    const bool in_grid = i < a.H && j < a.W;
+    const unsigned lane_base = tmem + ((unsigned)(warp * 32) << 16);
+#pragma unroll
+    for (int ch = 0; ch < BN / 16; ++ch) {
+      unsigned r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+          "[%16];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+            "=r"(r[14]), "=r"(r[15])
+          : "r"(lane_base + (unsigned)(ch * 16)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (!in_grid) continue;
+      bf16* o = a.out + (img + (long long)i * a.W + j) * a.out_cs;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int co = n0 + ch * 16 + h * 8;
+        if (co + 8 > a.cout) continue;
+        V8 prev, res;
+        if (a.accumulate) prev.u = *(const uint4*)(o + co);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float v0 = __uint_as_float(r[h * 8 + 2 * k]), v1 = __uint_as_float(r[h * 8 + 2 * k + 1]);
+          if (a.bias) {
+            v0 += a.bias[co + 2 * k];
+            v1 += a.bias[co + 2 * k + 1];
+          }
+          if (a.accumulate) {
+            const float2 f = __bfloat1622float2(prev.h[k]);
+            v0 += f.x;
+            v1 += f.y;
+          }
+          if (a.relu) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          res.h[k] = __floats2bfloat162_rn(v0, v1);
+        }
+        *(uint4*)(o + co) = res.u;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
+}
+
+static int g_conv_impl = 1;  // 1: tcgen05 (k_conv3_tc, default), 0: mma.sync (k_conv3)
+
+template <int BN>
+static int launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
+  constexpr int slab = TcGeom<BN>::SLAB;
+  static bool attr = false;
+  if (!attr) {
+    CEV_CUDA(cudaFuncSetAttribute(k_conv3_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * slab));
+    attr = true;
+  }
+  const int smem = (a.cinp > CBK ? 2 : 1) * slab;
+  const long long tiles = (long long)((a.H + HX_TI - 1) / HX_TI) * ((a.W + HX_TJ - 1) / HX_TJ) *
+                          (a.npix / ((long long)a.H * a.W));
+  k_conv3_tc<BN><<<dim3((unsigned)tiles, (a.cout + BN - 1) / BN), 128, smem, s>>>(a);
+  CEV_CHECK_LAUNCH("k_conv3_tc");
+  return CEV_OK;
+}
+
 static unsigned grid_for(long long n, int threads) {
   const long long want = (n + threads - 1) / threads;
   const long long cap = 16LL * sm_count();
@@ -643,6 +898,7 @@ struct cev_learned_precond_s {
   bf16* wd[NLAYER] = {};
   int cinp[NLAYER], coutp[NLAYER];
   float* nrm = nullptr;
+  double* rms_part = nullptr;  // [max_batch][RMS_PARTS]
   // activations (forward) and their gradients (backward, allocated on first use)
   enum { X0, A1, P1, A2, P2, A3, P3, A4, A5, A6, U3, A7, A8, U2, A9, A10, U1, A11, NACT };
   bf16* act[NACT] = {};
@@ -693,6 +949,10 @@ static int conv(Net& n, int l, const bf16* in, bf16* out, bool dgrad, int accumu
   a.relu = dgrad ? 0 : 1;
   a.accumulate = accumulate;
   const unsigned gx = (unsigned)((a.npix + CBM - 1) / CBM);
+  if (g_conv_impl == 1) {
+    if (a.cout <= 32) return launch_conv_tc<32>(a, s);
+    return launch_conv_tc<64>(a, s);
+  }
   if (a.cout <= 32) {
     k_conv3<32><<<dim3(gx, (a.cout + 31) / 32), 128, 0, s>>>(a);
   } else {
@@ -778,7 +1038,8 @@ int learned_forward(cev_learned_precond_s* hp, const cev_fdfd_plan_s* p, const f
   const int b = p->batch;
   n.batch = b;
   auto& A = n.act;
-  k_rms<<<b, 512, 0, s>>>(r, p->n(), n.nrm);
+  k_rms_part<<<dim3(RMS_PARTS, b), 256, 0, s>>>(r, p->n(), n.rms_part);
+  k_rms_final<<<(b + 127) / 128, 128, 0, s>>>(n.rms_part, p->n(), b, n.nrm);
   CEV_CHECK_LAUNCH("k_rms");
   k_prep<<<grid_for(n.npix(0, b), 256), 256, 0, s>>>(r, eps, eps_shared, p->k2_32, n.nrm, b, n.H[0],
                                                      n.W[0], p->npml_x, p->npml_y, A[Net::X0]);
@@ -924,6 +1185,7 @@ int cev_learned_create(cev_learned_precond* out, int nx, int ny, int max_batch, 
     if (rc == CEV_OK) rc = n->alloc(&n->wd[l], (size_t)9 * n->L[l].cin * n->coutp[l]);
   }
   if (rc == CEV_OK) rc = n->alloc(&n->nrm, (size_t)max_batch);
+  if (rc == CEV_OK) rc = n->alloc(&n->rms_part, (size_t)max_batch * RMS_PARTS);
   for (int k = 0; k < N::NACT && rc == CEV_OK; ++k) {
     n->act_c[k] = spec[k][0];
     n->act_lv[k] = spec[k][1];
@@ -980,6 +1242,20 @@ int cev_adam_step(float* p, const float* g, float* m, float* v, size_t n, float 
   const float bc1 = 1.f - powf(beta1, (float)step), bc2 = 1.f - powf(beta2, (float)step);
   k_adam<<<grid_for((long long)n, 256), 256, 0, s>>>(p, g, m, v, n, lr, beta1, beta2, eps, bc1, bc2);
   CEV_CHECK_LAUNCH("k_adam");
+  return CEV_OK;
+}
+
+int cev_learned_set_conv_impl(int impl) {
+  CEV_REQUIRE(impl == 0 || impl == 1, "conv implementation must be 0 (mma.sync) or 1 (tcgen05)");
+  g_conv_impl = impl;
+  return CEV_OK;
+}
+
+int cev_learned_tc_fault(int* fault) {
+  CEV_REQUIRE(fault != nullptr, "NULL argument");
+  int zero = 0;
+  CEV_CUDA(cudaMemcpyFromSymbol(fault, g_tc_fault, sizeof(int)));
+  CEV_CUDA(cudaMemcpyToSymbol(g_tc_fault, &zero, sizeof(int)));
   return CEV_OK;
 }
 

@@ -81,6 +81,33 @@ def test_forward_and_gradients_match_oracle(cev, shape):
         assert e_gpu <= 1.5 * e_ref + 1e-4, (kind, "head", e_gpu, e_ref)
 
 
+def test_conv_paths_agree(cev):
+    """The tcgen05 conv (default) and the mma.sync conv give the same forward
+    and backward up to accumulation order, and no bounded wait ran out."""
+    import ctypes as C
+    from ceviche_gb300 import _lib
+    from ceviche_gb300.learned import LearnedPreconditioner
+    lib = _lib.load()
+    nx, ny, B, c0 = 64, 48, 3, 32
+    plan, eps, r, p, k2, rng = _case(nx, ny, B, c0, seed=7)
+    net = LearnedPreconditioner(nx, ny, max_batch=4, c0=c0, params=p)
+    gz = torch.as_tensor(rng.standard_normal((B, nx, ny)) + 1j * rng.standard_normal((B, nx, ny)),
+                         dtype=torch.complex64).cuda()
+    out = {}
+    try:
+        for impl in (0, 1):
+            assert lib.cev_learned_set_conv_impl(impl) == 0
+            z = net.forward(plan, eps, r).cpu()
+            net.grad.zero_()
+            out[impl] = (z, net.backward(gz).cpu().clone())
+    finally:
+        lib.cev_learned_set_conv_impl(1)
+    fault = C.c_int(-1)
+    assert lib.cev_learned_tc_fault(C.byref(fault)) == 0 and fault.value == 0
+    assert _rel(out[1][0], out[0][0]) < 2e-3
+    assert _rel(out[1][1], out[0][1]) < 2e-2
+
+
 def test_training_gradient_through_stencil(cev):
     """loss_and_grad (network backward fed by the stencil adjoint) against
     torch autograd of the same physics loss with the dense A' and the
