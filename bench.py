@@ -441,6 +441,40 @@ def learned_numbers(train_problems=128, steps=6000, eval_batch=16, iter_cap=900)
                     "median residual at equal iteration counts is the comparison"}
 
 
+def learned_forward_numbers(conv_impl=1, steps=5, warmup=3, batch=16):
+    """Network forward of the learned preconditioner on `batch` config-4
+    problems of 256x256 (random-init weights; the cost does not depend on
+    them): time per forward and FLOP rate, for the tcgen05 or mma.sync conv."""
+    import torch
+    from ceviche_gb300 import _lib
+    from ceviche_gb300 import primitives as P
+    from ceviche_gb300.learned import LearnedPreconditioner
+    from ceviche_gb300.workloads import config4_problem
+    lib = _lib.load()
+    _lib.check(lib.cev_learned_set_conv_impl(conv_impl), "set_conv_impl")
+    probs = [config4_problem(i) for i in range(batch)]
+    oms = np.array([q["omega"] for q in probs])
+    plan = P.get_plan("ez", (256, 256), probs[0]["dL"], oms, probs[0]["npml"])
+    eps = torch.as_tensor(np.stack([q["eps"] for q in probs])).cuda()
+    r = torch.stack([torch.as_tensor(1j * q["omega"] * q["src"]) for q in probs]).cuda()
+    r = r.to(torch.complex64)
+    net = LearnedPreconditioner(256, 256, max_batch=batch, c0=32)
+    for _ in range(max(1, warmup)):
+        net.forward(plan, eps, r)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record()
+    for _ in range(steps):
+        net.forward(plan, eps, r)
+    end.record()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(end) / steps
+    flops = 2 * 66816 * batch * 256 * 256  # 7424 MACs x 9 taps per full-resolution pixel
+    return {"metric": "learned preconditioner forward", "conv_impl": ["mma.sync", "tcgen05"][conv_impl],
+            "batch": batch, "grid": [256, 256], "ms_per_forward": ms,
+            "tflops": flops / ms / 1e9, "steps": steps}
+
+
 def config_numbers(max_iters5=1500):
     """The other FDFD configurations with the plain GPU Krylov path (one JSON
     line, not part of the default run):
@@ -561,8 +595,14 @@ def main():
     ap.add_argument("--no-fdfd", action="store_true")
     ap.add_argument("--configs", action="store_true",
                     help="measure the other FDFD configurations (plain GPU Krylov) instead")
+    ap.add_argument("--learned-forward", action="store_true",
+                    help="time the learned preconditioner's network on 16 problems of 256x256")
+    ap.add_argument("--conv-impl", type=int, default=1, choices=[0, 1],
+                    help="with --learned-forward: 1 tcgen05 conv (default), 0 mma.sync conv")
     args = ap.parse_args()
-    if args.configs:
+    if args.learned_forward:
+        print(json.dumps(learned_forward_numbers(args.conv_impl, args.steps, args.warmup)), flush=True)
+    elif args.configs:
         print(json.dumps(config_numbers()), flush=True)
     elif args.impl == "reference":
         run_reference(args)

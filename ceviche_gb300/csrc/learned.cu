@@ -858,10 +858,215 @@ __global__ void __launch_bounds__(128) k_conv3_tc(ConvArgs a) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(BN));
 }
 
+// Persistent variant for single-slab layers (input channels <= 32): the
+// 9-tap weights stay resident in shared memory, halo tiles are double-
+// buffered and so are the TMEM accumulators (2 x BN columns), so while the
+// tensor cores run tile n the CTA stages tile n+1 and writes out tile n-1.
+template <int BN>
+__global__ void __launch_bounds__(128) k_conv3_tcp(ConvArgs a, int ntiles) {
+  extern __shared__ __align__(128) unsigned char tc_smem[];
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ unsigned tslot;
+  constexpr int TAP_B = TcGeom<BN>::TAP_B, SLAB_B = 9 * TAP_B;
+  constexpr unsigned IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(BN >> 3) << 17) |
+                             ((unsigned)(CBM >> 4) << 24);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tiles_j = (a.W + HX_TJ - 1) / HX_TJ, tiles_i = (a.H + HX_TI - 1) / HX_TI;
+  const int n0 = blockIdx.y * BN;
+  unsigned char* sbw = tc_smem;                // resident weights
+  unsigned char* sa0 = tc_smem + SLAB_B;       // two halo stages
+  const unsigned sbase = smem_u32(tc_smem);
+  if (tid == 0) {
+    for (int q = 0; q < 2; ++q)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[q])));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                     smem_u32(&tslot)),
+                 "r"(2 * BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const unsigned tmem = tslot;
+
+  auto tile_origin = [&](int t, long long& img, int& i0, int& j0) {
+    const int tj = t % tiles_j;
+    t /= tiles_j;
+    const int ti = t % tiles_i;
+    img = (long long)(t / tiles_i) * a.H * a.W;
+    i0 = ti * HX_TI;
+    j0 = tj * HX_TJ;
+  };
+  auto load_a = [&](int t, int st) {
+    long long img;
+    int i0, j0;
+    tile_origin(t, img, i0, j0);
+    unsigned char* sa = sa0 + st * HX_SLAB_A;
+    for (int e = tid; e < (CBK / 8) * HX_LINES; e += 128) {
+      const int c = e / HX_LINES, L = e - c * HX_LINES;
+      const int hr = L / HX_HJ, hc = L - hr * HX_HJ;
+      const int i = i0 - 1 + hr, j = j0 - 1 + hc, ch = c * 8;
+      const bool v = i >= 0 && i < a.H && j >= 0 && j < a.W && ch < a.cin;
+      const void* src =
+          v ? (const void*)(a.in + (img + (long long)i * a.W + j) * a.in_cs + ch) : (const void*)a.in;
+      cp_async16(sa + c * HX_LBO + L * 16, src, v);
+    }
+  };
+  auto epilogue = [&](int t, int buf) {
+    long long img;
+    int i0, j0;
+    tile_origin(t, img, i0, j0);
+    const int m = warp * 32 + lane;
+    const int i = i0 + m / HX_TJ, j = j0 + m % HX_TJ;
+    const bool in_grid = i < a.H && j < a.W;
+    const unsigned lane_base = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(buf * BN);
+#pragma unroll
+    for (int ch = 0; ch < BN / 16; ++ch) {
+      unsigned r[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+          "[%16];\n"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+            "=r"(r[14]), "=r"(r[15])
+          : "r"(lane_base + (unsigned)(ch * 16)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (!in_grid) continue;
+      bf16* o = a.out + (img + (long long)i * a.W + j) * a.out_cs;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int co = n0 + ch * 16 + h * 8;
+        if (co + 8 > a.cout) continue;
+        V8 prev, res;
+        if (a.accumulate) prev.u = *(const uint4*)(o + co);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float v0 = __uint_as_float(r[h * 8 + 2 * k]), v1 = __uint_as_float(r[h * 8 + 2 * k + 1]);
+          if (a.bias) {
+            v0 += a.bias[co + 2 * k];
+            v1 += a.bias[co + 2 * k + 1];
+          }
+          if (a.accumulate) {
+            const float2 f = __bfloat1622float2(prev.h[k]);
+            v0 += f.x;
+            v1 += f.y;
+          }
+          if (a.relu) {
+            v0 = fmaxf(v0, 0.f);
+            v1 = fmaxf(v1, 0.f);
+          }
+          res.h[k] = __floats2bfloat162_rn(v0, v1);
+        }
+        *(uint4*)(o + co) = res.u;
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  };
+
+  // resident weights + the first tile, one cp.async group
+  for (int e = tid; e < 9 * BN * (CBK / 8); e += 128) {
+    const int c = e & 3, rt = e >> 2;
+    const int row = rt % BN, tap = rt / BN;
+    const int co = n0 + row;
+    const bool v = co < a.cout;
+    const void* src = v ? (const void*)(a.w + ((size_t)tap * a.cout + co) * a.cinp + c * 8) : (const void*)a.w;
+    cp_async16(sbw + tap * TAP_B + (row >> 3) * 512 + (row & 7) * 16 + c * 128, src, v);
+  }
+  const int first = blockIdx.x;
+  if (first < ntiles) load_a(first, 0);
+  cp_commit();
+
+  bool ok = true;
+  int n = 0, issued = -1;
+  for (int t = first; t < ntiles && ok; t += gridDim.x, ++n) {
+    const int st = n & 1;
+    cp_wait_all();
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const unsigned sa = sbase + (unsigned)(SLAB_B + st * HX_SLAB_A), sb = sbase;
+      const unsigned dcol = tmem + (unsigned)(st * BN);
+#pragma unroll
+      for (int tap = 0; tap < 9; ++tap) {
+        const unsigned aoff = (unsigned)(((tap / 3) * HX_HJ + (tap % 3)) * 16);
+#pragma unroll
+        for (int kk = 0; kk < CBK / 16; ++kk) {
+          const unsigned long long ad = tc_desc(sa + kk * 2 * HX_LBO + aoff, HX_LBO, HX_SBO);
+          const unsigned long long bd = tc_desc(sb + tap * TAP_B + kk * 256, 128, 512);
+          const unsigned acc = (tap > 0 || kk > 0) ? 1u : 0u;
+          asm volatile(
+              "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dcol),
+              "l"(ad), "l"(bd), "r"(IDESC), "r"(acc));
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_u32(&mbar[st]))
+                   : "memory");
+    }
+    issued = n;
+    // tile n-1: its MMAs read stage st^1 and wrote TMEM buffer st^1
+    bool w = true;
+    if (n >= 1) w = mbar_wait(smem_u32(&mbar[st ^ 1]), (unsigned)(((n - 1) >> 1) & 1));
+    ok = __syncthreads_and(w ? 1 : 0) != 0;
+    if (!ok) break;
+    const int next = t + gridDim.x;
+    if (next < ntiles) load_a(next, st ^ 1);
+    cp_commit();
+    if (n >= 1) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      epilogue(t - gridDim.x, st ^ 1);
+    }
+  }
+  // the last committed tile; its commit also covers every earlier MMA, so
+  // after a timeout this waits (bounded) for whatever is still in flight
+  if (issued >= 0) {
+    const bool done = mbar_wait(smem_u32(&mbar[issued & 1]), (unsigned)((issued >> 1) & 1));
+    ok = ok && done;
+    const int all_ok = __syncthreads_and(ok ? 1 : 0);
+    if (all_ok) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      epilogue(first + issued * (int)gridDim.x, issued & 1);
+    }
+  }
+  cp_wait_all();
+  if (!ok) atomicExch(&g_tc_fault, 1);
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * BN));
+}
+
 static int g_conv_impl = 1;  // 1: tcgen05 (k_conv3_tc, default), 0: mma.sync (k_conv3)
+static int g_conv_nonpersistent = 0;  // 1: single-slab layers also use k_conv3_tc
+
+template <int BN>
+static int launch_conv_tcp(const ConvArgs& a, cudaStream_t s) {
+  constexpr int smem = 9 * TcGeom<BN>::TAP_B + 2 * HX_SLAB_A;
+  static int per_sm = 0;
+  if (!per_sm) {
+    CEV_CUDA(cudaFuncSetAttribute(k_conv3_tcp<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    CEV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tcp<BN>, 128, smem));
+    // TMEM: 2*BN columns per CTA out of 512
+    per_sm = std::max(1, std::min(per_sm, 512 / (2 * BN)));
+  }
+  const long long tiles = (long long)((a.H + HX_TI - 1) / HX_TI) * ((a.W + HX_TJ - 1) / HX_TJ) *
+                          (a.npix / ((long long)a.H * a.W));
+  const int ny = (a.cout + BN - 1) / BN;
+  const long long cap = std::max(1LL, (long long)per_sm * sm_count() / ny);
+  const unsigned gx = (unsigned)std::min(tiles, cap);
+  k_conv3_tcp<BN><<<dim3(gx, ny), 128, smem, s>>>(a, (int)tiles);
+  CEV_CHECK_LAUNCH("k_conv3_tcp");
+  return CEV_OK;
+}
 
 template <int BN>
 static int launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
+  if (a.cinp == CBK && !g_conv_nonpersistent) return launch_conv_tcp<BN>(a, s);
   constexpr int slab = TcGeom<BN>::SLAB;
   static bool attr = false;
   if (!attr) {
@@ -1246,8 +1451,10 @@ int cev_adam_step(float* p, const float* g, float* m, float* v, size_t n, float 
 }
 
 int cev_learned_set_conv_impl(int impl) {
-  CEV_REQUIRE(impl == 0 || impl == 1, "conv implementation must be 0 (mma.sync) or 1 (tcgen05)");
-  g_conv_impl = impl;
+  CEV_REQUIRE(impl >= 0 && impl <= 2,
+              "conv implementation must be 0 (mma.sync), 1 (tcgen05) or 2 (tcgen05, not persistent)");
+  g_conv_impl = impl == 0 ? 0 : 1;
+  g_conv_nonpersistent = impl == 2 ? 1 : 0;
   return CEV_OK;
 }
 

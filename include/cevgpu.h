@@ -180,8 +180,9 @@ CEV_API int cev_learned_backward(cev_learned_precond h, const void* gz, float* g
                                  cudaStream_t stream);
 CEV_API int cev_adam_step(float* p, const float* g, float* m, float* v, size_t n, float lr,
                           float beta1, float beta2, float eps, int step, cudaStream_t stream);
-/* Convolution kernels: 1 = tcgen05 with TMEM accumulators (default),
- * 0 = mma.sync.  cev_learned_tc_fault reads and clears the flag the tcgen05
+/* Convolution kernels: 1 = tcgen05 with TMEM accumulators (default; layers
+ * with <= 32 input channels run a persistent variant), 2 = tcgen05 without
+ * the persistent variant, 0 = mma.sync.  cev_learned_tc_fault reads and clears the flag the tcgen05
  * kernel sets when one of its bounded waits ran out (synchronises). */
 CEV_API int cev_learned_set_conv_impl(int impl);
 CEV_API int cev_learned_tc_fault(int* fault);
