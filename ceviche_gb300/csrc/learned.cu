@@ -1050,9 +1050,10 @@ static int launch_conv_tcp(const ConvArgs& a, cudaStream_t s) {
   static int per_sm = 0;
   if (!per_sm) {
     CEV_CUDA(cudaFuncSetAttribute(k_conv3_tcp<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    CEV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tcp<BN>, 128, smem));
-    // TMEM: 2*BN columns per CTA out of 512
-    per_sm = std::max(1, std::min(per_sm, 512 / (2 * BN)));
+    CEV_CUDA(cudaFuncSetAttribute(k_conv3_tcp<BN>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    // resident CTAs per SM: shared memory (227 KB usable, 1 KB reserved per
+    // CTA) and TMEM (2*BN of 512 columns per CTA)
+    per_sm = std::max(1, std::min((227 * 1024) / (smem + 128 + 1024), 512 / (2 * BN)));
   }
   const long long tiles = (long long)((a.H + HX_TI - 1) / HX_TI) * ((a.W + HX_TJ - 1) / HX_TJ) *
                           (a.npix / ((long long)a.H * a.W));
