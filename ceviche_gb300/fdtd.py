@@ -57,7 +57,7 @@ class fdtd:
         self._destroy()
 
     def _destroy(self):
-        if getattr(self, "_plan_h", None) is not None and _lib._lib is not None:
+        if getattr(self, "_plan_h", None) is not None and getattr(_lib, "_lib", None) is not None:
             _lib._lib.cev_fdtd_plan_destroy(self._plan_h)
             self._plan_h = None
 

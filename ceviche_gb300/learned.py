@@ -81,7 +81,7 @@ class LearnedPreconditioner:
 
     def __del__(self):
         h = getattr(self, "handle", None)
-        if h is not None and _lib._lib is not None:
+        if h is not None and getattr(_lib, "_lib", None) is not None:
             _lib._lib.cev_learned_destroy(h)
             self.handle = None
 
@@ -183,4 +183,20 @@ def residual_samples(plan, eps, b, iters=(0, 10, 30, 90)):
                 done = k
             r = bt if x is None else bt - P.apply(plan, eps, x)
             out.append(r.to(torch.complex64))
+    return out
+
+
+def on_policy_samples(net, plan, eps, b, iters=(30, 90, 270)):
+    """Residuals b - A x_k of flexible GMRES *with the network* after k
+    iterations: the vectors on which the preconditioned solver stalls.  One
+    round of training on these (with the plain-solver samples) lowers the
+    residual the preconditioned solver reaches."""
+    bt = P._field_arg(plan, b, torch.complex128)
+    out = []
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", P.SolverWarning)
+        for k in iters:
+            x, _ = P.solve(plan, eps, bt, tol=1e-14, max_iters=k, max_stall=10 ** 6,
+                           precond="learned", learned=net)
+            out.append((bt - P.apply(plan, eps, x)).to(torch.complex64))
     return out

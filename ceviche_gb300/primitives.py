@@ -58,7 +58,7 @@ class Plan:
 
     def __del__(self):
         h = getattr(self, "handle", None)
-        if h is not None and _lib._lib is not None:
+        if h is not None and getattr(_lib, "_lib", None) is not None:
             _lib._lib.cev_fdfd_plan_destroy(h)
             self.handle = None
 
@@ -173,11 +173,40 @@ class SolveResult(list):
     """Per-problem solve records (status, iterations, cycles, residual)."""
 
 
-def solve(plan, eps, b, transpose=False, x0=None, strict=False, **opts):
+def solve(plan, eps, b, transpose=False, x0=None, strict=False, fallback=True, **opts):
     """Solve A x = b (A^T x = b) for every problem; b complex (batch, nx, ny) in SI units.
 
     Returns (x complex128, infos).  Non-convergence warns (or raises with strict).
+    With a preconditioner (``precond`` "learned" or "separable") and
+    ``fallback``, a solve that stops short of ``tol`` (stagnation of the
+    flexible GMRES) continues with plain GMRES from its iterate for the rest of
+    the ``max_iters`` budget; the infos then count both phases and record the
+    preconditioned iterations as ``precond_iterations``.
     """
+    x, res, rc, tol = _solve_once(plan, eps, b, transpose, x0, **opts)
+    if rc > 0 and fallback and opts.get("precond", "none") not in ("none", 0):
+        left = int(opts.get("max_iters", _DEFAULT_OPTS["max_iters"])) - max(r["iterations"] for r in res)
+        if left > 0:
+            plain = {k: v for k, v in opts.items() if k not in ("precond", "learned", "separable")}
+            plain["max_iters"] = left
+            x, res2, rc, tol = _solve_once(plan, eps, b, transpose, x, **plain)
+            for r, r2 in zip(res, res2):
+                r2["precond_iterations"] = r["iterations"]
+                r2["iterations"] += r["iterations"]
+                r2["cycles"] += r["cycles"]
+            res = res2
+    if rc > 0:
+        msg = (f"FDFD solve did not reach tol={tol:g}: "
+               + ", ".join(f"[{k}] {r['status']} res={r['residual']:.3g} it={r['iterations']}"
+                           for k, r in enumerate(res) if r["code"] != 0))
+        if strict:
+            raise _lib.CevError(msg)
+        warnings.warn(msg, SolverWarning, stacklevel=2)
+    return x, res
+
+
+def _solve_once(plan, eps, b, transpose, x0, **opts):
+    """One cev_fdfd_solve call: (x, infos, status, tol)."""
     lib = _lib.load()
     e, sh = _eps_arg(plan, eps, torch.float64)
     bt = _field_arg(plan, b, torch.complex128)
@@ -203,14 +232,7 @@ def solve(plan, eps, b, transpose=False, x0=None, strict=False, **opts):
                            iterations=i.iterations, cycles=i.cycles, residual=i.residual)
                       for i in infos)
     del ws
-    if rc > 0:
-        msg = (f"FDFD solve did not reach tol={s.tol:g}: "
-               + ", ".join(f"[{k}] {r['status']} res={r['residual']:.3g} it={r['iterations']}"
-                           for k, r in enumerate(res) if r["code"] != 0))
-        if strict:
-            raise _lib.CevError(msg)
-        warnings.warn(msg, SolverWarning, stacklevel=2)
-    return x, res
+    return x, res, rc, s.tol
 
 
 def fields(plan, eps, fz):
@@ -328,7 +350,7 @@ class SeparablePrecond:
 
     def __del__(self):
         h = getattr(self, "handle", None)
-        if h is not None and _lib._lib is not None:
+        if h is not None and getattr(_lib, "_lib", None) is not None:
             _lib._lib.cev_sep_precond_destroy(h)
             self.handle = None
 
@@ -424,7 +446,7 @@ class MFPlan:
 
     def __del__(self):
         h = getattr(self, "handle", None)
-        if h is not None and _lib._lib is not None:
+        if h is not None and getattr(_lib, "_lib", None) is not None:
             _lib._lib.cev_fdfd_plan_destroy(h)
             self.handle = None
 

@@ -226,3 +226,36 @@ def test_invalid_uses_fail(cev):
     two = P.get_plan("ez", (32, 32), 50e-9, [1.2e15, 1.3e15], (4, 4))
     with pytest.raises(CevError):
         P.solve(two, eps, b.expand(2, 32, 32), precond="learned", learned=net)  # batch > max
+
+
+def test_dropin_class_with_learned_preconditioner(cev):
+    """fdfd_ez(..., precond="learned") with an untrained network: flexible
+    GMRES stagnates and the solver falls back to plain GMRES from its iterate;
+    the field and the eps-gradient (adjoint solve, same fallback) match the
+    oracle's."""
+    from ceviche_gb300.learned import LearnedPreconditioner
+    rng = np.random.default_rng(11)
+    nx, ny, npml, dL = 40, 32, 6, 40e-9
+    omega = 2 * np.pi * 3e8 / 1.5e-6
+    eps = rng.uniform(1, 4, (nx, ny))
+    src = np.zeros((nx, ny))
+    src[10, 12:20] = 1.0
+    net = LearnedPreconditioner(nx, ny, max_batch=1, c0=8, seed=3)
+    F = cev.fdfd_ez(omega, dL, torch.as_tensor(eps, device="cuda"), [npml, npml], tol=1e-10,
+                    precond="learned", learned=net)
+    e = torch.tensor(eps, device="cuda", requires_grad=True)
+    F.eps_r = e
+    _, _, ez = F.solve(torch.as_tensor(src, device="cuda"))
+    A = ofd.make_A_ez(omega, dL, eps, [npml, npml])
+    ref = ofd.spsolve(A, 1j * omega * src.ravel())
+    assert np.linalg.norm(ez.detach().cpu().numpy().ravel() - ref) <= 1e-8 * np.linalg.norm(ref)
+    probe = np.zeros((nx, ny))
+    probe[30, 10:22] = 1.0
+    J = (ez * torch.as_tensor(probe, device="cuda")).sum().abs() ** 2
+    J.backward()
+    s = np.sum(ref * probe.ravel())
+    g_ez = 2 * np.conj(s) * probe  # dJ/dRe + i dJ/dIm of |sum(Ez * probe)|^2
+    zeros = np.zeros((nx, ny))
+    g_ref = ofd.grad_eps_ez(omega, dL, eps, [npml, npml], src, zeros, zeros, g_ez.conj())
+    g = e.grad.cpu().numpy()
+    assert np.linalg.norm(g - g_ref) <= 1e-6 * np.linalg.norm(g_ref), np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref)
