@@ -436,23 +436,55 @@ struct XupArgs {
   KCtx ctx;
 };
 
+// S + E += (h + l) * v with h*v exact (FMA TwoProd) and the sum by Knuth's
+// TwoSum: a float-float accumulation on the FP32 pipe (GB300's FP64 rate
+// would make a double accumulation of 30+ terms per cell the bottleneck of
+// this otherwise bandwidth-bound kernel).
+__device__ __forceinline__ void ff_acc(float& S, float& E, float h, float l, float v) {
+  const float p = __fmul_rn(h, v);
+  const float e = __fadd_rn(__fmaf_rn(h, v, -p), __fmul_rn(l, v));
+  const float t = __fadd_rn(S, p);
+  const float bb = __fsub_rn(t, S);
+  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+  S = t;
+  E = __fadd_rn(E, __fadd_rn(err, e));
+}
+
 __global__ void __launch_bounds__(RED_THREADS) k_xupdate(XupArgs a) {
   const int b = blockIdx.y;
   const KState* st = a.ctx.st + b;
   const int k = st->ncols;
   if (k == 0 || st->done) return;
-  __shared__ double2 cy[64];
+  // y_q (times the basis scale) can lie far outside the float range (tiny or
+  // huge right-hand sides), so the float-float sum runs on y_q / ymax and
+  // the FP64 result is scaled back by ymax.
+  __shared__ double2 yd[64];
+  __shared__ float4 cy[64];  // (re hi, re lo, im hi, im lo) of y_q / ymax
+  __shared__ double ymax;
   for (int q = threadIdx.x; q < k; q += blockDim.x) {
     double2 yy = a.ctx.y[(size_t)b * a.m + q];
     if (!a.flexible) yy = cscale(yy, a.ctx.sc[(size_t)b * (a.m + 1) + q]);
-    cy[q] = yy;
+    yd[q] = yy;
   }
   __syncthreads();
+  if (threadIdx.x == 0) {
+    double mx = 0.0;
+    for (int q = 0; q < k; ++q) mx = fmax(mx, fmax(fabs(yd[q].x), fabs(yd[q].y)));
+    ymax = (mx > 0.0 && mx < INFINITY) ? mx : 1.0;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    const double yr = yd[q].x / ymax, yi = yd[q].y / ymax;
+    const float rh = (float)yr, ih = (float)yi;
+    cy[q] = make_float4(rh, (float)(yr - (double)rh), ih, (float)(yi - (double)ih));
+  }
+  __syncthreads();
+  const double ys = ymax;
   const float2* base = a.flexible ? a.Z : a.V;
   double2* x = a.x + b * a.n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t n = (size_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += stride) {
-    double2 acc = make_double2(0.0, 0.0);
+    float sr = 0.f, er = 0.f, si = 0.f, ei = 0.f;
     constexpr int G = 8;
     for (int q0 = 0; q0 < k; q0 += G) {
       float2 v[G];
@@ -460,12 +492,19 @@ __global__ void __launch_bounds__(RED_THREADS) k_xupdate(XupArgs a) {
       for (int q = 0; q < G; ++q)
         v[q] = (q0 + q < k) ? base[((size_t)(q0 + q) * a.B + b) * a.n + n] : make_float2(0.f, 0.f);
 #pragma unroll
-      for (int q = 0; q < G; ++q)
-        if (q0 + q < k) acc = cfma(cy[q0 + q], to_d(v[q]), acc);
+      for (int q = 0; q < G; ++q) {
+        if (q0 + q >= k) break;
+        const float4 y = cy[q0 + q];
+        ff_acc(sr, er, y.x, y.y, v[q].x);    // + Re y Re v
+        ff_acc(sr, er, -y.z, -y.w, v[q].y);  // - Im y Im v
+        ff_acc(si, ei, y.x, y.y, v[q].y);    // + Re y Im v
+        ff_acc(si, ei, y.z, y.w, v[q].x);    // + Im y Re v
+      }
     }
     // The cycle solved A' d = r with A' = scale*A and r the residual of
     // A' x = scale*b, so d is already a correction of x in SI units.
-    x[n] = cadd(x[n], acc);
+    const double2 xo = x[n];
+    x[n] = make_double2(xo.x + ys * ((double)sr + (double)er), xo.y + ys * ((double)si + (double)ei));
   }
 }
 
@@ -487,7 +526,7 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 int fused_max_blocks() { return 2 * sm_count(); }
 
 int reduction_blocks(size_t n, int B) {
-  const long target = 4L * sm_count();
+  const long target = 8L * sm_count();
   long nb = (target + B - 1) / B;
   long cap = (long)((n + RED_THREADS - 1) / RED_THREADS);
   return (int)std::max(1L, std::min(nb, cap));
