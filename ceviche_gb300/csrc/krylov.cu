@@ -633,7 +633,7 @@ int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opt
     for (int b = 0; b < B; ++b) {
       KState& q = hst[b];
       if (q.fault) {
-        set_error("a bounded device wait of the fused GMRES cycle timed out");
+        set_error("a bounded device wait (fused GMRES cycle or TMA matvec) timed out");
         return CEV_ERR_CUDA;
       }
       if (q.done) continue;
@@ -792,8 +792,12 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
     CEV_CHECK_LAUNCH("k_residual");
     return CEV_OK;
   };
+  const bool tma_mv = tma_matvec_usable(p, ce);
   ops.matvec = [&](const KCtx& c, int j, const float2* in, int use_scale, float2* out,
                    cudaStream_t st) -> int {
+    // TMA needs 16-byte aligned operands; anything else takes the column sweep
+    if (tma_mv && (((uintptr_t)in | (uintptr_t)eps32) & 15) == 0)
+      return tma_matvec_ez(p, tr, eps32, eps_shared, in, out, c, m, j, use_scale, st);
     auto go = [&](auto pol_tag, auto e_tag) {
       constexpr int POL = decltype(pol_tag)::value;
       using E = decltype(e_tag);
