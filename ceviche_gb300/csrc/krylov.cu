@@ -797,7 +797,7 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
                    cudaStream_t st) -> int {
     // TMA needs 16-byte aligned operands; anything else takes the column sweep
     if (tma_mv && (((uintptr_t)in | (uintptr_t)eps32) & 15) == 0)
-      return tma_matvec_ez(p, tr, eps32, eps_shared, in, out, c, m, j, use_scale, st);
+      return tma_matvec(p, tr, eps32, eps_shared, in, out, c, m, j, use_scale, st);
     auto go = [&](auto pol_tag, auto e_tag) {
       constexpr int POL = decltype(pol_tag)::value;
       using E = decltype(e_tag);

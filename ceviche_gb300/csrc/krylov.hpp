@@ -113,11 +113,11 @@ int precond_setup(Precond& pc, const cev_fdfd_plan_s* p, const cev_solve_opts& o
 int precond_apply(Precond& pc, const KCtx& c, int j, int m, const float2* v, float2* z,
                   cudaStream_t s);
 
-// TMA-staged Arnoldi matvec (csrc/stencil_tma.cu): Ez, real eps, ny % 4 == 0
+// TMA-staged Arnoldi matvec (csrc/stencil_tma.cu): Ez and Hz, real eps, ny % 4 == 0
 bool tma_matvec_usable(const cev_fdfd_plan_s* p, bool eps_complex);
-int tma_matvec_ez(const cev_fdfd_plan_s* p, int tr, const float* eps32, int eps_shared,
-                  const float2* in, float2* out, const KCtx& c, int m, int j, int use_scale,
-                  cudaStream_t s);
+int tma_matvec(const cev_fdfd_plan_s* p, int tr, const float* eps32, int eps_shared,
+               const float2* in, float2* out, const KCtx& c, int m, int j, int use_scale,
+               cudaStream_t s);
 
 namespace nn {
 int learned_check(const cev_learned_precond_s* h, const cev_fdfd_plan_s* p);

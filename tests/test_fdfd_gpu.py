@@ -294,10 +294,11 @@ def test_fused_cycle_batch(cev, shared_eps, monkeypatch):
         assert abs(a_ - b_) <= 0.1 * b_ + 2, (itf, itm)
 
 
+@pytest.mark.parametrize("pol", ["ez", "hz"])
 @pytest.mark.parametrize("shape,bloch", [((40, 132), (0.0, 0.0)), ((40, 132), (0.7, -1.1)),
                                          ((16, 8), (0.3, 0.5)), ((33, 256), (0.0, 0.4))])
-def test_tma_matvec_matches_column_sweep(cev, shape, bloch, monkeypatch):
-    """The TMA-staged Arnoldi matvec (Ez, real eps, ny % 4 == 0) against the
+def test_tma_matvec_matches_column_sweep(cev, pol, shape, bloch, monkeypatch):
+    """The TMA-staged Arnoldi matvec (Ez and Hz, real eps, ny % 4 == 0) against the
     column-sweep kernel in the per-iteration GMRES path: partial row and
     column tiles, Bloch phases on the periodic wrap, forward and transposed
     solves, a two-frequency batch; both reach the FP64 tolerance (1e-7)
@@ -309,7 +310,7 @@ def test_tma_matvec_matches_column_sweep(cev, shape, bloch, monkeypatch):
     oms = 2 * np.pi * 3e8 / np.array([1.5e-6, 1.7e-6])
     eps = rng.uniform(1, 5, (2, Nx, Ny))
     b = rng.standard_normal((2, Nx, Ny)) + 1j * rng.standard_normal((2, Nx, Ny))
-    plan = P.get_plan("ez", (Nx, Ny), dL, oms, npml, bloch=bloch)
+    plan = P.get_plan(pol, (Nx, Ny), dL, oms, npml, bloch=bloch)
     monkeypatch.setenv("CEV_FUSED_CYCLE", "0")
     out = {}
     for tma in ("1", "0"):
@@ -318,7 +319,7 @@ def test_tma_matvec_matches_column_sweep(cev, shape, bloch, monkeypatch):
             x, info = P.solve(plan, torch.as_tensor(eps), torch.as_tensor(b), transpose=tr, tol=1e-7,
                               strict=True)
             for k, w in enumerate(oms):
-                A = ofd.make_A("ez", w, dL, eps[k], npml, bloch)
+                A = ofd.make_A(pol, w, dL, eps[k], npml, bloch)
                 A = A.T if tr else A
                 assert ofd.true_residual(A, x[k].cpu().numpy().ravel(), b[k].ravel()) < 1e-7
             out[tma, tr] = x.cpu().numpy()
