@@ -181,7 +181,10 @@ def solve(plan, eps, b, transpose=False, x0=None, strict=False, fallback=True, *
     ``fallback``, a solve that stops short of ``tol`` (stagnation of the
     flexible GMRES) continues with plain GMRES from its iterate for the rest of
     the ``max_iters`` budget; the infos then count both phases and record the
-    preconditioned iterations as ``precond_iterations``.
+    preconditioned iterations as ``precond_iterations``.  ``max_stall`` sets
+    when the preconditioned phase hands over (a small value gives a hybrid:
+    the network for the first cycles, plain GMRES after); the plain phase
+    keeps at least the default stall limit.
     """
     x, res, rc, tol = _solve_once(plan, eps, b, transpose, x0, **opts)
     if rc > 0 and fallback and opts.get("precond", "none") not in ("none", 0):
@@ -189,6 +192,10 @@ def solve(plan, eps, b, transpose=False, x0=None, strict=False, fallback=True, *
         if left > 0:
             plain = {k: v for k, v in opts.items() if k not in ("precond", "learned", "separable")}
             plain["max_iters"] = left
+            # the stall limit decides when to leave the preconditioned phase; the
+            # plain phase keeps at least the default patience
+            plain["max_stall"] = max(int(opts.get("max_stall", _DEFAULT_OPTS["max_stall"])),
+                                     _DEFAULT_OPTS["max_stall"])
             x, res2, rc, tol = _solve_once(plan, eps, b, transpose, x, **plain)
             for r, r2 in zip(res, res2):
                 r2["precond_iterations"] = r["iterations"]

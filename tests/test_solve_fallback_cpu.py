@@ -34,10 +34,19 @@ def test_fallback_continues_with_plain(fake):
     assert len(calls) == 2
     x0, opts = calls[1]
     assert "precond" not in opts and "learned" not in opts and opts["max_iters"] == 700
+    assert opts["max_stall"] == 20  # default patience for the plain phase
     assert torch.equal(x0, torch.full((1, 2, 2), 1.0))  # continues from the first iterate
     assert torch.equal(x, torch.full((1, 2, 2), 2.0))
     assert res[0]["iterations"] == 420 and res[0]["precond_iterations"] == 300
     assert res[0]["cycles"] == 14 and res[0]["code"] == 0
+
+
+def test_hybrid_stall_limit_only_governs_the_handover(fake):
+    P, calls = fake
+    P.solve(None, None, None, precond="learned", learned=object(), max_stall=1, max_iters=1000)
+    assert calls[0][1]["max_stall"] == 1 and calls[1][1]["max_stall"] == 20
+    P.solve(None, None, None, precond="learned", learned=object(), max_stall=50, max_iters=1000)
+    assert calls[3][1]["max_stall"] == 50
 
 
 def test_no_fallback_without_preconditioner_or_when_disabled(fake):
