@@ -23,11 +23,13 @@
 // contiguous), the grid's own (i, j) order.  Parameters are one fp32 vector:
 // per conv layer W[cout][cin][3][3] then b[cout]; then the head W[2][c0], b[2].
 //
-// Tensor-core path: the 3x3 convs are implicit GEMMs on mma.sync m16n8k16
-// (bf16 in, fp32 accumulate), operands staged in shared memory by cp.async
-// and read with ldmatrix.  The data gradient is the same kernel with the
-// weights flipped and transposed; the weight gradient is a second GEMM that
-// reduces over pixels (split over blocks, fp32 atomics).
+// Tensor-core paths: the 3x3 convs are implicit GEMMs (bf16 in, fp32
+// accumulate).  By default they run on tcgen05 with TMEM accumulators
+// (k_conv3_tc, and k_conv3_tcp for single-slab layers).  k_conv3 is the
+// mma.sync m16n8k16 alternative: cp.async staging, ldmatrix operands.  The
+// data gradient is the same conv with the weights flipped and transposed.
+// The weight gradient (k_wgrad3, mma.sync) is a second GEMM that reduces
+// over pixels, split over blocks, with fp32 atomics.
 #include <cuda_bf16.h>
 
 #include <algorithm>
