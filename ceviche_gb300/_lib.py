@@ -19,7 +19,7 @@ CEV_NOT_CONVERGED = 1
 CEV_STAGNATED = 2
 POL_EZ, POL_HZ = 0, 1
 PREC_C64, PREC_C128 = 0, 1
-PRECOND = {"none": 0, "shifted_laplacian": 1, "learned": 2, "separable": 3}
+PRECOND = {"none": 0, "shifted_laplacian": 1, "learned": 2, "separable": 3, "direct": 4}
 STATUS_NAMES = {0: "converged", 1: "not converged", 2: "stagnated", -1: "invalid argument",
                 -2: "CUDA error", -3: "workspace", -4: "non-finite values"}
 
@@ -29,7 +29,7 @@ class SolveOpts(C.Structure):
                 ("restart", C.c_int), ("precond", C.c_int), ("transpose", C.c_int),
                 ("use_x0", C.c_int), ("reorth", C.c_int), ("max_stall", C.c_int),
                 ("mg_levels", C.c_int), ("mg_shift", C.c_double), ("learned", C.c_void_p),
-                ("separable", C.c_void_p)]
+                ("separable", C.c_void_p), ("direct", C.c_void_p)]
 
 
 class SolveInfo(C.Structure):
@@ -63,6 +63,12 @@ SIGNATURES = {
     "cev_fdfd_plan_set_eps_complex": (I, [P, I]),
     "cev_sep_precond_create": (I, [PP, P, I, P, P, P, P, P]),
     "cev_sep_precond_destroy": (I, [P]),
+    "cev_nd_precond_create": (I, [PP, P, P, I, I, D, P]),
+    "cev_nd_precond_apply": (I, [P, P, P, P]),
+    "cev_nd_precond_info": (I, [P, C.POINTER(S), C.POINTER(D), C.POINTER(I)]),
+    "cev_nd_precond_destroy": (I, [P]),
+    "cev_nd_analyse": (I, [I, I, C.POINTER(S), C.POINTER(I), C.POINTER(S), C.POINTER(D),
+                           C.POINTER(S), C.POINTER(C.c_longlong)]),
     "cev_learned_param_count": (I, [I, C.POINTER(S)]),
     "cev_learned_create": (I, [PP, I, I, I, I]),
     "cev_learned_set_params": (I, [P, P, P]),

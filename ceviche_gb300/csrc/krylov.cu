@@ -685,6 +685,13 @@ int krylov_run(const KrylovProblem& P, const KrylovOps& ops, const cev_solve_opt
         k_update<<<rg, RED_THREADS, 0, s>>>(ua);
       }
       CEV_CHECK_LAUNCH("arnoldi step");
+      if (ops.check_each_step && j + 1 < m) {
+        CEV_CUDA(cudaMemcpyAsync(hst.data(), c.st, sizeof(KState) * B, cudaMemcpyDeviceToHost, s));
+        CEV_CUDA(cudaStreamSynchronize(s));
+        bool left = false;
+        for (int b = 0; b < B; ++b) left = left || hst[b].active;
+        if (!left) break;
+      }
     }
     k_trisolve<<<B, 64, 0, s>>>(c, B, m);
     XupArgs xa{N, B, m, flexible ? 1 : 0, V, Z, xvec, 1.0, c};
@@ -711,7 +718,8 @@ int validate_opts(const cev_solve_opts& o) {
   CEV_REQUIRE(o.tol > 0 && o.tol < 1, "tol must be in (0, 1)");
   CEV_REQUIRE(o.max_iters >= 1, "max_iters must be >= 1");
   CEV_REQUIRE(o.precond == CEV_PRECOND_NONE || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN ||
-                  o.precond == CEV_PRECOND_LEARNED || o.precond == CEV_PRECOND_SEPARABLE,
+                  o.precond == CEV_PRECOND_LEARNED || o.precond == CEV_PRECOND_SEPARABLE ||
+                  o.precond == CEV_PRECOND_DIRECT,
               "unknown preconditioner %d", o.precond);
   return CEV_OK;
 }
@@ -737,6 +745,7 @@ void cev_solve_opts_default(cev_solve_opts* o) {
   o->mg_shift = 0.5;
   o->learned = nullptr;
   o->separable = nullptr;
+  o->direct = nullptr;
 }
 
 size_t cev_fdfd_solve_workspace_size(cev_fdfd_plan p, const cev_solve_opts* opts) {
@@ -839,6 +848,8 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
     ops.precond = [&](const KCtx& c, int j, const float2* v, float2* z, cudaStream_t st) {
       return precond_apply(pc, c, j, m, v, z, st);
     };
+    ops.check_each_step =
+        o.precond == CEV_PRECOND_DIRECT || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN;
   }
   return krylov_run(P, ops, o, (const double2*)bvec, (double2*)xvec, info, ws, ws_bytes, s);
 }

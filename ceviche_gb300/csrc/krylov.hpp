@@ -72,6 +72,10 @@ struct KrylovOps {
   // one launch (replaces the per-iteration matvec / dot / update launches).
   std::function<int(const KCtx&, float2* V, cudaStream_t)> cycle;
   double bscale = 1.0;
+  // The preconditioner costs far more than a host round trip: after every
+  // Arnoldi step the driver reads the problems' activity and ends the cycle
+  // once none is left (a converging direct preconditioner needs few steps).
+  bool check_each_step = false;
 };
 
 // Fused stencil cycle for small batches (cycle.cu).
@@ -118,6 +122,12 @@ bool tma_matvec_usable(const cev_fdfd_plan_s* p, bool eps_complex);
 int tma_matvec(const cev_fdfd_plan_s* p, int tr, const float* eps32, int eps_shared,
                const float2* in, float2* out, const KCtx& c, int m, int j, int use_scale,
                cudaStream_t s);
+
+// Nested-dissection factors (csrc/nd.cu): z = M^-1 (sc[b][sc_index] v) for
+// the problems whose Arnoldi work is still on (st may be NULL: all).
+int nd_apply(cev_nd_precond_s* h, const float2* v, float2* z, const double* sc, int sc_stride,
+             int sc_index, const KState* st, cudaStream_t s);
+int nd_check(const cev_nd_precond_s* h, const cev_fdfd_plan_s* p, int kind, int transpose);
 
 namespace nn {
 int learned_check(const cev_learned_precond_s* h, const cev_fdfd_plan_s* p);

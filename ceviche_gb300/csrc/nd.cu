@@ -1,0 +1,1117 @@
+// Nested-dissection multifrontal factorisation of the FDFD stencil system in
+// complex64: the right preconditioner CEV_PRECOND_DIRECT of flexible GMRES,
+// and, built with a shift beta, the exact shifted-operator inverse behind
+// CEV_PRECOND_SHIFTED_LAPLACIAN.
+//
+// ceviche reaches its solutions with a sparse direct solve
+// (ceviche/solvers.py:50-62, scipy SuperLU).  Here the same kind of
+// factorisation is a preconditioner: M = A' without the periodic wrap
+// entries, factored in complex64 without pivoting; the FP64 true residual of
+// the flexible GMRES decides convergence, so the complex64 rounding of the
+// factors (and the dropped wrap) only adds iterations (typically 2-4 to 1e-6).
+//
+// Ordering.  The (nx, ny) grid is split recursively: a box splits its longer
+// side at the midpoint by a one-cell separator line; boxes with both sides
+// <= LEAF are eliminated whole.  A node of the tree eliminates its interior
+// set I (the separator, or all cells of a leaf box) and couples to its
+// boundary set B (the one-cell frame around its box, inside the grid), which
+// is always a subset of ancestor separators.  The front of a node is the
+// dense matrix F over [I; B]:
+//   F = A'(I, I u B), A'(B, I)  +  the children's Schur complements (extend-add).
+// Gauss-Jordan sweeps of the I pivots turn F into
+//   [[ G = F_II^-1,  H = G F_IB ],
+//    [ -K = -F_BI G,  S = F_BB - F_BI G F_IB ]]
+// (the block "sweep operator").  S is the node's update matrix for its parent;
+// G, H, -K are kept.  Applying M^-1 v is then GEMVs only:
+//   forward (leaves first):  f = [v_I ; 0] + sum children's u,  u = f_B - K f_I
+//   backward (root first):   x_I = G f_I - H x_B.
+//
+// Storage (per problem, complex64): the per-node row block [G | H] (nI x f,
+// row-major) and -K (nB x nI); per depth, depth-major, so one depth of all
+// problems is one contiguous range.  Schur complements live in two arenas
+// alternating by depth parity (a node's children are one depth deeper).
+//
+// Kernels.  Fronts with f <= 128 (the lower levels, most nodes) are assembled
+// and swept entirely in shared memory, one CTA per (node, problem), each
+// thread holding its block of F in registers.  Larger fronts are assembled in
+// global memory and swept in blocks of NB = 32 pivots: invert the pivot block,
+// scale the pivot rows, a rank-32 update of every other entry (64 x 64 tiles,
+// FP32 FMA), and scale the pivot columns; the rank-32 update carries the
+// flops.  The apply kernels are bandwidth-bound GEMVs over the factor (warp
+// per row, coalesced along the rows).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "fdfd_plan.hpp"
+#include "krylov.hpp"
+
+namespace cev {
+namespace nd {
+
+constexpr int LEAF = 4;        // boxes with both sides <= LEAF are eliminated whole
+constexpr int NB = 32;         // pivots per block step of the large-front path
+constexpr int SMALL_F = 128;   // fronts up to this size are swept in shared memory
+constexpr int TILE = 64;       // update tile (rows x cols) of the large-front path
+constexpr int GEMV_ROWS = 32;  // rows per CTA of the apply GEMVs
+
+struct Node {
+  int nI, nB;
+  int cells;         // offset in the cell list: nI interior then nB boundary cells
+  int child[2];      // -1: none
+  int cmap[2];       // offset in the map list: child's B cells -> positions in this front
+  int desc, ndesc;   // original-entry descriptors
+  int par;           // Schur arena of this node's depth (depth & 1)
+  int pad;
+  long long top;     // [G | H] (nI x f) of problem 0; problem b adds b * fst
+  long long bl;      // -K (nB x nI) of problem 0
+  long long fst;     // factor stride between problems at this depth
+  long long s;       // S (nB x nB) in arena par, problem 0; problem b adds b * sst
+  long long sst;
+  long long fv;      // front vector (f) of problem 0; problem b adds b * fvst
+  long long fvst;
+};
+
+// A'(row cell, neighbour in direction dir) of one stencil row:
+// dir 0 = diagonal, 1 = (i-1, j), 2 = (i+1, j), 3 = (i, j-1), 4 = (i, j+1).
+struct Desc {
+  int row, col, cell, dir;
+};
+
+// What defines the entries: the plan's float tables for one transpose flag.
+struct Op {
+  int pol, nx, ny;
+  int eps_complex;
+  size_t eps_bs;  // eps batch stride in elements (0: shared)
+  const double* eps;
+  const Coef<float>* cx;  // [B][nx]
+  const Coef<float>* cy;  // [B][ny]
+  const float* k2;        // [B]
+  float shift;            // mass term times (1 - i shift)
+};
+
+struct Args {
+  Op op;
+  const Node* nodes;
+  const int* cells;
+  const int* cmap;
+  const Desc* desc;
+  float2* fac;
+  float2* sar[2];
+  float2* fv;
+  int* fault;  // set when a pivot is zero or not finite
+  size_t n;    // cells per problem
+};
+
+__device__ __forceinline__ float2 eps_at(const Op& o, int b, int i, int j) {
+  i = (i + o.nx) % o.nx;
+  j = (j + o.ny) % o.ny;
+  const size_t k = (size_t)b * o.eps_bs + (size_t)i * o.ny + j;
+  if (o.eps_complex) return make_float2((float)o.eps[2 * k], (float)o.eps[2 * k + 1]);
+  return make_float2((float)o.eps[k], 0.f);
+}
+
+// 1/((a + b)/2 + 1e-5) in complex arithmetic (the Hz averages of fdfd.py:200-233)
+__device__ __forceinline__ float2 hzd(float2 a, float2 b) {
+  const float2 den = make_float2(0.5f * (a.x + b.x) + 1e-5f, 0.5f * (a.y + b.y));
+  const float q = 1.0f / (den.x * den.x + den.y * den.y);
+  return make_float2(den.x * q, -den.y * q);
+}
+
+// The entry of A' (the same arithmetic as stencil_column in stencil.cuh, with
+// the mass term times (1 - i shift)).
+__device__ float2 coef(const Op& o, int b, int cell, int dir) {
+  const int i = cell / o.ny, j = cell - (cell / o.ny) * o.ny;
+  const Coef<float> cx = o.cx[(size_t)b * o.nx + i];
+  const Coef<float> cy = o.cy[(size_t)b * o.ny + j];
+  const float k2 = o.k2[b];
+  const float2 sh = make_float2(1.f, -o.shift);
+  if (o.pol == POL_EZ) {
+    switch (dir) {
+      case 1: return make_float2(-cx.cm.x, -cx.cm.y);
+      case 2: return make_float2(-cx.cp.x, -cx.cp.y);
+      case 3: return make_float2(-cy.cm.x, -cy.cm.y);
+      case 4: return make_float2(-cy.cp.x, -cy.cp.y);
+      default: {
+        const float2 d0 = cadd(cadd(cx.am, cx.ap), cadd(cy.am, cy.ap));
+        const float2 m = cmul(cscale(eps_at(o, b, i, j), k2), sh);
+        return csub(d0, m);
+      }
+    }
+  }
+  const float2 e = eps_at(o, b, i, j);
+  switch (dir) {
+    case 1: return cmul(cx.cm, hzd(eps_at(o, b, i - 1, j), eps_at(o, b, i - 2, j)));
+    case 2: return cmul(cx.cp, hzd(e, eps_at(o, b, i - 1, j)));
+    case 3: return cmul(cy.cm, hzd(eps_at(o, b, i, j - 1), eps_at(o, b, i, j - 2)));
+    case 4: return cmul(cy.cp, hzd(e, eps_at(o, b, i, j - 1)));
+    default: {
+      const float2 dyym = hzd(eps_at(o, b, i - 1, j), eps_at(o, b, i - 2, j));
+      const float2 dyyp = hzd(e, eps_at(o, b, i - 1, j));
+      const float2 dxxm = hzd(eps_at(o, b, i, j - 1), eps_at(o, b, i, j - 2));
+      const float2 dxxp = hzd(e, eps_at(o, b, i, j - 1));
+      const float2 d0 = cadd(cadd(cmul(cx.am, dyym), cmul(cx.ap, dyyp)),
+                             cadd(cmul(cy.am, dxxm), cmul(cy.ap, dxxp)));
+      return csub(cscale(sh, k2), d0);
+    }
+  }
+}
+
+__device__ __forceinline__ float2 crcp(float2 d) {
+  const float q = 1.0f / (d.x * d.x + d.y * d.y);
+  return make_float2(d.x * q, -d.y * q);
+}
+
+__device__ __forceinline__ void check_pivot(const Args& a, float2 d) {
+  const float m = d.x * d.x + d.y * d.y;
+  if (!(m > 0.f) || !isfinite(m)) atomicExch(a.fault, 1);
+}
+
+// Address of front entry (r, c) of node n for problem b (large-front path).
+__device__ __forceinline__ float2* fel(const Args& a, const Node& n, int b, int r, int c) {
+  const int f = n.nI + n.nB;
+  if (r < n.nI) return a.fac + n.top + (long long)b * n.fst + (long long)r * f + c;
+  r -= n.nI;
+  if (c < n.nI) return a.fac + n.bl + (long long)b * n.fst + (long long)r * n.nI + c;
+  return a.sar[n.par] + n.s + (long long)b * n.sst + (long long)r * n.nB + (c - n.nI);
+}
+
+// ============================================================ small fronts
+// One CTA per (node, problem): assemble F (f <= FS) in shared memory, keep
+// each thread's TR x TC-strided block of it in registers through the
+// Gauss-Jordan sweep, write [G | H], -K and S out.
+template <int FS, int TR, int TC>
+__global__ void __launch_bounds__(TR * TC) k_small(Args a, const int* __restrict__ list) {
+  constexpr int R = FS / TR, Cn = FS / TC;
+  extern __shared__ float2 sm[];
+  float2* F = sm;                // f x f, row stride f
+  float2* rowbuf = sm + FS * FS;  // FS
+  float2* colbuf = rowbuf + FS;   // FS
+  __shared__ float2 s_pinv;
+  const Node n = a.nodes[list[blockIdx.x]];
+  const int b = blockIdx.y;
+  const int f = n.nI + n.nB, nI = n.nI, nB = n.nB;
+  const int tid = threadIdx.x, nt = TR * TC;
+  for (int e = tid; e < f * f; e += nt) F[e] = make_float2(0.f, 0.f);
+  __syncthreads();
+  for (int q = tid; q < n.ndesc; q += nt) {
+    const Desc d = a.desc[n.desc + q];
+    const float2 v = coef(a.op, b, d.cell, d.dir);
+    float2& t = F[d.row * f + d.col];
+    t = cadd(t, v);
+  }
+  __syncthreads();
+  for (int s = 0; s < 2; ++s) {
+    if (n.child[s] < 0) continue;
+    const Node c = a.nodes[n.child[s]];
+    const int* map = a.cmap + n.cmap[s];
+    const float2* S = a.sar[c.par] + c.s + (long long)b * c.sst;
+    for (int e = tid; e < c.nB * c.nB; e += nt) {
+      const int r = e / c.nB, q = e - r * c.nB;
+      float2& t = F[map[r] * f + map[q]];
+      t = cadd(t, S[e]);
+    }
+    __syncthreads();
+  }
+  const int ty = tid / TC, tx = tid - (tid / TC) * TC;
+  float2 reg[R][Cn];
+#pragma unroll
+  for (int u = 0; u < R; ++u)
+#pragma unroll
+    for (int v = 0; v < Cn; ++v) {
+      const int r = ty + TR * u, c = tx + TC * v;
+      reg[u][v] = (r < f && c < f) ? F[r * f + c] : make_float2(0.f, 0.f);
+    }
+  for (int p = 0; p < nI; ++p) {
+    // the owner of (p, p) publishes 1/F_pp
+    if ((p % TR) == ty && (p % TC) == tx) {
+      float2 d = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int u = 0; u < R; ++u)
+#pragma unroll
+        for (int v = 0; v < Cn; ++v)
+          if (ty + TR * u == p && tx + TC * v == p) d = reg[u][v];
+      check_pivot(a, d);
+      s_pinv = crcp(d);
+    }
+    __syncthreads();
+    const float2 pinv = s_pinv;
+#pragma unroll
+    for (int u = 0; u < R; ++u)
+#pragma unroll
+      for (int v = 0; v < Cn; ++v) {
+        const int r = ty + TR * u, c = tx + TC * v;
+        if (r == p && c != p && c < f) rowbuf[c] = cmul(reg[u][v], pinv);
+        if (c == p && r != p && r < f) colbuf[r] = reg[u][v];
+      }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const int r = ty + TR * u;
+      if (r >= f) continue;
+      const float2 cr = colbuf[r];
+#pragma unroll
+      for (int v = 0; v < Cn; ++v) {
+        const int c = tx + TC * v;
+        if (c >= f) continue;
+        if (r == p) {
+          reg[u][v] = (c == p) ? pinv : rowbuf[c];
+        } else if (c == p) {
+          const float2 t = cmul(cr, pinv);
+          reg[u][v] = make_float2(-t.x, -t.y);
+        } else {
+          const float2 rc = rowbuf[c];
+          reg[u][v].x -= cr.x * rc.x - cr.y * rc.y;
+          reg[u][v].y -= cr.x * rc.y + cr.y * rc.x;
+        }
+      }
+    }
+  }
+  float2* top = a.fac + n.top + (long long)b * n.fst;
+  float2* bl = a.fac + n.bl + (long long)b * n.fst;
+  float2* S = a.sar[n.par] + n.s + (long long)b * n.sst;
+#pragma unroll
+  for (int u = 0; u < R; ++u)
+#pragma unroll
+    for (int v = 0; v < Cn; ++v) {
+      const int r = ty + TR * u, c = tx + TC * v;
+      if (r >= f || c >= f) continue;
+      if (r < nI) top[(size_t)r * f + c] = reg[u][v];
+      else if (c < nI) bl[(size_t)(r - nI) * nI + c] = reg[u][v];
+      else S[(size_t)(r - nI) * nB + (c - nI)] = reg[u][v];
+    }
+}
+
+// ============================================================ large fronts
+// Original entries of the large fronts (fronts zeroed beforehand).
+__global__ void k_orig(Args a, const int* __restrict__ list) {
+  const Node n = a.nodes[list[blockIdx.x]];
+  const int b = blockIdx.y;
+  for (int q = threadIdx.x; q < n.ndesc; q += blockDim.x) {
+    const Desc d = a.desc[n.desc + q];
+    float2* t = fel(a, n, b, d.row, d.col);
+    *t = cadd(*t, coef(a.op, b, d.cell, d.dir));
+  }
+}
+
+// Extend-add of one child's Schur complement, one child row per CTA
+// (work: node index, child row).
+__global__ void k_extend(Args a, const int2* __restrict__ work, int slot) {
+  const int2 w = work[blockIdx.x];
+  const Node n = a.nodes[w.x];
+  const int b = blockIdx.y;
+  const Node c = a.nodes[n.child[slot]];
+  const int* map = a.cmap + n.cmap[slot];
+  const int r = w.y;
+  const float2* S = a.sar[c.par] + c.s + (long long)b * c.sst + (long long)r * c.nB;
+  const int pr = map[r];
+  for (int q = threadIdx.x; q < c.nB; q += blockDim.x) {
+    float2* t = fel(a, n, b, pr, map[q]);
+    *t = cadd(*t, S[q]);
+  }
+}
+
+// In-place inverse of the pivot block F[k0:k0+nb, k0:k0+nb] (Gauss-Jordan).
+__global__ void __launch_bounds__(256) k_pivblock(Args a, const int* __restrict__ list, int k0) {
+  __shared__ float2 blk[NB][NB + 1];
+  __shared__ float2 rowb[NB], colb[NB];
+  __shared__ float2 s_pinv;
+  const Node n = a.nodes[list[blockIdx.x]];
+  if (k0 >= n.nI) return;
+  const int b = blockIdx.y;
+  const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
+  float2* base = a.fac + n.top + (long long)b * n.fst;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int r = e / nb, c = e - r * nb;
+    blk[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
+  }
+  __syncthreads();
+  for (int p = 0; p < nb; ++p) {
+    if (threadIdx.x == 0) {
+      check_pivot(a, blk[p][p]);
+      s_pinv = crcp(blk[p][p]);
+    }
+    __syncthreads();
+    const float2 pinv = s_pinv;
+    if (threadIdx.x < nb) {
+      rowb[threadIdx.x] = cmul(blk[p][threadIdx.x], pinv);
+      colb[threadIdx.x] = blk[threadIdx.x][p];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+      const int r = e / nb, c = e - r * nb;
+      if (r == p) {
+        blk[r][c] = (c == p) ? pinv : rowb[c];
+      } else if (c == p) {
+        const float2 t = cmul(colb[r], pinv);
+        blk[r][c] = make_float2(-t.x, -t.y);
+      } else {
+        const float2 t = cmul(colb[r], rowb[c]);
+        blk[r][c] = csub(blk[r][c], t);
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int r = e / nb, c = e - r * nb;
+    base[(size_t)(k0 + r) * f + k0 + c] = blk[r][c];
+  }
+}
+
+// Pivot rows: F[p, c] = Ainv F[p, c] for the 64 columns of one chunk outside
+// the pivot block (work: node index, column chunk).
+__global__ void __launch_bounds__(256) k_rowpanel(Args a, const int2* __restrict__ work, int k0) {
+  __shared__ float2 Ai[NB][NB + 1];
+  __shared__ float2 P[NB][TILE + 1];
+  const int2 w = work[blockIdx.x];
+  const Node n = a.nodes[w.x];
+  if (k0 >= n.nI) return;
+  const int b = blockIdx.y;
+  const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
+  const int c0 = w.y * TILE;
+  float2* base = a.fac + n.top + (long long)b * n.fst;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int r = e / nb, c = e - r * nb;
+    Ai[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
+  }
+  for (int e = threadIdx.x; e < nb * TILE; e += blockDim.x) {
+    const int r = e / TILE, c = e - r * TILE;
+    const int gc = c0 + c;
+    P[r][c] = (gc < f) ? base[(size_t)(k0 + r) * f + gc] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nb * TILE; e += blockDim.x) {
+    const int r = e / TILE, c = e - r * TILE;
+    const int gc = c0 + c;
+    if (gc >= f || (gc >= k0 && gc < k0 + nb)) continue;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int k = 0; k < nb; ++k) acc = cfma(Ai[r][k], P[k][c], acc);
+    base[(size_t)(k0 + r) * f + gc] = acc;
+  }
+}
+
+// Rank-nb update of every entry outside the pivot rows and columns:
+// F[r, c] -= F[r, p] R[p, c], one 64 x 64 tile per CTA (work: node, tile).
+// 128 threads, each an 8 x 4 block of the tile (rows ty + 8u, cols tx + 16v).
+__global__ void __launch_bounds__(128) k_update(Args a, const int2* __restrict__ work, int k0) {
+  __shared__ float2 Cp[TILE][NB + 1];
+  __shared__ float2 Rp[NB][TILE];
+  const int2 w = work[blockIdx.x];
+  const Node n = a.nodes[w.x];
+  if (k0 >= n.nI) return;
+  const int b = blockIdx.y;
+  const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
+  const int tiles = (f + TILE - 1) / TILE;
+  const int r0 = (w.y / tiles) * TILE, c0 = (w.y % tiles) * TILE;
+  // column panel F[r0 + i, k0 + k] (rows may be I or B rows; k0 + k < nI)
+  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
+    const int i = e / NB, k = e - i * NB;
+    const int r = r0 + i;
+    Cp[i][k] = (r < f && k < nb) ? *fel(a, n, b, r, k0 + k) : make_float2(0.f, 0.f);
+  }
+  const float2* rows = a.fac + n.top + (long long)b * n.fst;
+  for (int e = threadIdx.x; e < NB * TILE; e += blockDim.x) {
+    const int k = e / TILE, j = e - k * TILE;
+    const int c = c0 + j;
+    Rp[k][j] = (k < nb && c < f) ? rows[(size_t)(k0 + k) * f + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  float2 acc[8][4];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+#pragma unroll 4
+  for (int k = 0; k < NB; ++k) {
+    float2 cv[8], rv[4];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) cv[u] = Cp[ty + 8 * u][k];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) rv[v] = Rp[k][tx + 16 * v];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        acc[u][v].x = fmaf(cv[u].x, rv[v].x, acc[u][v].x);
+        acc[u][v].x = fmaf(-cv[u].y, rv[v].y, acc[u][v].x);
+        acc[u][v].y = fmaf(cv[u].x, rv[v].y, acc[u][v].y);
+        acc[u][v].y = fmaf(cv[u].y, rv[v].x, acc[u][v].y);
+      }
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int r = r0 + ty + 8 * u;
+    if (r >= f || (r >= k0 && r < k0 + nb)) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int c = c0 + tx + 16 * v;
+      if (c >= f || (c >= k0 && c < k0 + nb)) continue;
+      float2* t = fel(a, n, b, r, c);
+      *t = csub(*t, acc[u][v]);
+    }
+  }
+}
+
+// Pivot columns: F[r, p] = -F[r, p] Ainv for the 64 rows of one chunk
+// outside the pivot block (work: node index, row chunk).
+__global__ void __launch_bounds__(256) k_colpanel(Args a, const int2* __restrict__ work, int k0) {
+  __shared__ float2 Ai[NB][NB + 1];
+  __shared__ float2 P[TILE][NB + 1];
+  const int2 w = work[blockIdx.x];
+  const Node n = a.nodes[w.x];
+  if (k0 >= n.nI) return;
+  const int b = blockIdx.y;
+  const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
+  const int r0 = w.y * TILE;
+  const float2* base = a.fac + n.top + (long long)b * n.fst;
+  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
+    const int r = e / nb, c = e - r * nb;
+    Ai[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
+  }
+  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
+    const int i = e / NB, k = e - i * NB;
+    const int r = r0 + i;
+    P[i][k] = (r < f && k < nb) ? *fel(a, n, b, r, k0 + k) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
+    const int i = e / NB, k = e - i * NB;
+    const int r = r0 + i;
+    if (k >= nb || r >= f || (r >= k0 && r < k0 + nb)) continue;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int q = 0; q < nb; ++q) acc = cfma(P[i][q], Ai[q][k], acc);
+    *fel(a, n, b, r, k0 + k) = make_float2(-acc.x, -acc.y);
+  }
+}
+
+// ================================================================ apply
+struct ApplyIO {
+  const float2* v;   // [B][n] input (Krylov basis vector)
+  float2* z;         // [B][n] output
+  const double* sc;  // per-problem input scale sc[b * sc_stride + sc_index] (NULL: 1)
+  int sc_stride, sc_index;
+  const KState* st;  // skip problems whose Arnoldi work is off (NULL: none)
+};
+
+__device__ __forceinline__ bool skip(const ApplyIO& io, int b) {
+  return io.st != nullptr && !io.st[b].active;
+}
+
+// Forward gather: f = [s v_I ; 0] + children's update vectors, written to the
+// node's front vector; with GEMV, also u = f_B + (-K) f_I (small fronts).
+template <bool GEMV>
+__global__ void __launch_bounds__(256) k_fwd(Args a, ApplyIO io, const int* __restrict__ list) {
+  extern __shared__ float2 fvs[];
+  const Node n = a.nodes[list[blockIdx.x]];
+  const int b = blockIdx.y;
+  if (skip(io, b)) return;
+  const int f = n.nI + n.nB;
+  const float s = io.sc ? (float)io.sc[(size_t)b * io.sc_stride + io.sc_index] : 1.f;
+  const int* cl = a.cells + n.cells;
+  const float2* v = io.v + (size_t)b * a.n;
+  for (int t = threadIdx.x; t < f; t += blockDim.x)
+    fvs[t] = t < n.nI ? cscale(v[cl[t]], s) : make_float2(0.f, 0.f);
+  __syncthreads();
+  for (int sl = 0; sl < 2; ++sl) {
+    if (n.child[sl] < 0) continue;
+    const Node c = a.nodes[n.child[sl]];
+    const int* map = a.cmap + n.cmap[sl];
+    const float2* u = a.fv + c.fv + (long long)b * c.fvst + c.nI;
+    for (int t = threadIdx.x; t < c.nB; t += blockDim.x) {
+      float2& d = fvs[map[t]];
+      d = cadd(d, u[t]);
+    }
+    __syncthreads();
+  }
+  float2* out = a.fv + n.fv + (long long)b * n.fvst;
+  if (GEMV) {
+    const float2* K = a.fac + n.bl + (long long)b * n.fst;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int r = warp; r < n.nB; r += nw) {
+      float2 acc = make_float2(0.f, 0.f);
+      const float2* row = K + (size_t)r * n.nI;
+      for (int k = lane; k < n.nI; k += 32) acc = cfma(row[k], fvs[k], acc);
+      acc.x = warp_sumf(acc.x);
+      acc.y = warp_sumf(acc.y);
+      if (lane == 0) out[n.nI + r] = cadd(fvs[n.nI + r], acc);
+    }
+    for (int t = threadIdx.x; t < n.nI; t += blockDim.x) out[t] = fvs[t];
+  } else {
+    for (int t = threadIdx.x; t < f; t += blockDim.x) out[t] = fvs[t];
+  }
+}
+
+// Forward GEMV of a large front: u[r] += (-K)[r] f_I for GEMV_ROWS rows
+// (work: node, row chunk).
+__global__ void __launch_bounds__(256) k_fwd_gemv(Args a, ApplyIO io, const int2* __restrict__ work) {
+  extern __shared__ float2 fi[];
+  const int2 w = work[blockIdx.x];
+  const Node n = a.nodes[w.x];
+  const int b = blockIdx.y;
+  if (skip(io, b)) return;
+  float2* fvn = a.fv + n.fv + (long long)b * n.fvst;
+  for (int t = threadIdx.x; t < n.nI; t += blockDim.x) fi[t] = fvn[t];
+  __syncthreads();
+  const float2* K = a.fac + n.bl + (long long)b * n.fst;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int r1 = min(n.nB, (w.y + 1) * GEMV_ROWS);
+  for (int r = w.y * GEMV_ROWS + warp; r < r1; r += nw) {
+    float2 acc = make_float2(0.f, 0.f);
+    const float2* row = K + (size_t)r * n.nI;
+    for (int k = lane; k < n.nI; k += 32) acc = cfma(row[k], fi[k], acc);
+    acc.x = warp_sumf(acc.x);
+    acc.y = warp_sumf(acc.y);
+    if (lane == 0) fvn[n.nI + r] = cadd(fvn[n.nI + r], acc);
+  }
+}
+
+// Backward: x_I = [G | H] [f_I ; -x_B] for GEMV_ROWS rows (work: node, row chunk).
+__global__ void __launch_bounds__(256) k_bwd(Args a, ApplyIO io, const int2* __restrict__ work) {
+  extern __shared__ float2 wv[];
+  const int2 w = work[blockIdx.x];
+  const Node n = a.nodes[w.x];
+  const int b = blockIdx.y;
+  if (skip(io, b)) return;
+  const int f = n.nI + n.nB;
+  const float2* fvn = a.fv + n.fv + (long long)b * n.fvst;
+  const int* cl = a.cells + n.cells;
+  float2* z = io.z + (size_t)b * a.n;
+  for (int t = threadIdx.x; t < f; t += blockDim.x) {
+    if (t < n.nI) {
+      wv[t] = fvn[t];
+    } else {
+      const float2 x = z[cl[t]];
+      wv[t] = make_float2(-x.x, -x.y);
+    }
+  }
+  __syncthreads();
+  const float2* T = a.fac + n.top + (long long)b * n.fst;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int r1 = min(n.nI, (w.y + 1) * GEMV_ROWS);
+  for (int r = w.y * GEMV_ROWS + warp; r < r1; r += nw) {
+    float2 acc = make_float2(0.f, 0.f);
+    const float2* row = T + (size_t)r * f;
+    for (int k = lane; k < f; k += 32) acc = cfma(row[k], wv[k], acc);
+    acc.x = warp_sumf(acc.x);
+    acc.y = warp_sumf(acc.y);
+    if (lane == 0) z[cl[r]] = acc;
+  }
+}
+
+// ============================================================ host side
+struct HNode {
+  int x0, x1, y0, y1, depth, parent;
+  int child[2] = {-1, -1};
+  std::vector<int> I, B;
+};
+
+struct Level {
+  std::vector<int> small, large;            // node ids
+  std::vector<int2> ext[2], panel, tiles;   // large-front work lists
+  std::vector<int2> gemv, bwd;              // apply work lists
+  int max_f_small = 0, max_f = 0, max_nI_large = 0, max_nI = 0;
+  long long fac_stride = 0, s_stride = 0, fv_stride = 0;
+  // device copies
+  int *d_small = nullptr, *d_large = nullptr;
+  int2 *d_ext[2] = {nullptr, nullptr}, *d_panel = nullptr, *d_tiles = nullptr;
+  int2 *d_gemv = nullptr, *d_bwd = nullptr;
+};
+
+class Tree {
+ public:
+  int nx, ny;
+  std::vector<HNode> nodes;
+  int build(int x0, int x1, int y0, int y1, int depth, int parent) {
+    if (x1 <= x0 || y1 <= y0) return -1;
+    const int id = (int)nodes.size();
+    nodes.push_back(HNode());
+    {
+      HNode& h = nodes.back();
+      h.x0 = x0; h.x1 = x1; h.y0 = y0; h.y1 = y1; h.depth = depth; h.parent = parent;
+    }
+    const int w = x1 - x0, hh = y1 - y0;
+    std::vector<int> I;
+    int c0 = -1, c1 = -1;
+    if (w <= LEAF && hh <= LEAF) {
+      for (int i = x0; i < x1; ++i)
+        for (int j = y0; j < y1; ++j) I.push_back(i * ny + j);
+    } else if (w >= hh) {
+      const int xs = x0 + w / 2;
+      for (int j = y0; j < y1; ++j) I.push_back(xs * ny + j);
+      c0 = build(x0, xs, y0, y1, depth + 1, id);
+      c1 = build(xs + 1, x1, y0, y1, depth + 1, id);
+    } else {
+      const int ys = y0 + hh / 2;
+      for (int i = x0; i < x1; ++i) I.push_back(i * ny + ys);
+      c0 = build(x0, x1, y0, ys, depth + 1, id);
+      c1 = build(x0, x1, ys + 1, y1, depth + 1, id);
+    }
+    std::vector<int> B;
+    if (x0 > 0) for (int j = y0; j < y1; ++j) B.push_back((x0 - 1) * ny + j);
+    if (x1 < nx) for (int j = y0; j < y1; ++j) B.push_back(x1 * ny + j);
+    if (y0 > 0) for (int i = x0; i < x1; ++i) B.push_back(i * ny + y0 - 1);
+    if (y1 < ny) for (int i = x0; i < x1; ++i) B.push_back(i * ny + y1);
+    HNode& h = nodes[id];
+    h.I = std::move(I);
+    h.B = std::move(B);
+    int k = 0;
+    if (c0 >= 0) h.child[k++] = c0;
+    if (c1 >= 0) h.child[k++] = c1;
+    return id;
+  }
+};
+
+}  // namespace nd
+}  // namespace cev
+
+using namespace cev;
+using namespace cev::nd;
+
+struct cev_nd_precond_s {
+  int nx = 0, ny = 0, batch = 0, pol = 0, transpose = 0, device = 0;
+  double shift = 0;
+  size_t n = 0;
+  int ndepth = 0;
+  std::vector<Level> levels;
+  Node* d_nodes = nullptr;
+  int* d_cells = nullptr;
+  int* d_cmap = nullptr;
+  Desc* d_desc = nullptr;
+  float2* fac = nullptr;
+  float2* sar[2] = {nullptr, nullptr};
+  float2* fv = nullptr;
+  int* fault = nullptr;
+  size_t fac_elems = 0, sar_elems[2] = {0, 0}, fv_elems = 0;
+  double flops = 0;  // complex multiply-adds of the factorisation, all problems
+  const cev_fdfd_plan_s* plan = nullptr;
+  ~cev_nd_precond_s() {
+    for (auto& L : levels) {
+      cudaFree(L.d_small); cudaFree(L.d_large); cudaFree(L.d_ext[0]); cudaFree(L.d_ext[1]);
+      cudaFree(L.d_panel); cudaFree(L.d_tiles); cudaFree(L.d_gemv); cudaFree(L.d_bwd);
+    }
+    cudaFree(d_nodes); cudaFree(d_cells); cudaFree(d_cmap); cudaFree(d_desc);
+    cudaFree(fac); cudaFree(sar[0]); cudaFree(sar[1]); cudaFree(fv); cudaFree(fault);
+  }
+};
+
+namespace cev {
+namespace nd {
+
+template <typename T>
+static int upload(T** dst, const std::vector<T>& v) {
+  *dst = nullptr;
+  if (v.empty()) return CEV_OK;
+  CEV_CUDA(cudaMalloc((void**)dst, sizeof(T) * v.size()));
+  CEV_CUDA(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  return CEV_OK;
+}
+
+// Dynamic shared memory above the 48 KB default, once per device and kernel.
+static int allow_smem(const void* fn, int slot, int bytes) {
+  static std::mutex mu;
+  static int done[64][8] = {};
+  int dev = 0;
+  CEV_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64 || slot < 0 || slot >= 8) return CEV_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(mu);
+  if (done[dev][slot] >= bytes) return CEV_OK;
+  CEV_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done[dev][slot] = bytes;
+  return CEV_OK;
+}
+
+// Builds the tree, offsets, descriptors, maps and work lists; uploads them
+// when `upload_all` (otherwise only the sizes are filled in: no CUDA call).
+static int analyse(cev_nd_precond_s* h, bool upload_all, size_t* n_nodes = nullptr,
+                   size_t* n_desc = nullptr, long long* cover = nullptr) {
+  Tree t;
+  t.nx = h->nx;
+  t.ny = h->ny;
+  t.nodes.reserve(2 * (size_t)h->nx * h->ny / (LEAF * LEAF) + 16);
+  t.build(0, h->nx, 0, h->ny, 0, -1);
+  const int nn = (int)t.nodes.size();
+  int maxd = 0;
+  for (auto& x : t.nodes) maxd = std::max(maxd, x.depth);
+  h->ndepth = maxd + 1;
+  h->levels.assign(h->ndepth, Level());
+  std::vector<Node> dn(nn);
+  std::vector<int> cells, cmap;
+  std::vector<Desc> desc;
+  std::vector<int> pos((size_t)h->nx * h->ny, -1);
+  // per-depth offsets
+  std::vector<long long> fac_off(h->ndepth, 0), s_off(h->ndepth, 0), fv_off(h->ndepth, 0);
+  std::vector<std::vector<int>> by_depth(h->ndepth);
+  for (int k = 0; k < nn; ++k) by_depth[t.nodes[k].depth].push_back(k);
+  const long long B = h->batch;
+  long long fac_base = 0, fv_base = 0;
+  const int nx = h->nx, ny = h->ny;
+  double flops = 0;
+  for (int d = 0; d < h->ndepth; ++d) {
+    Level& L = h->levels[d];
+    long long fo = 0, so = 0, vo = 0;
+    for (int k : by_depth[d]) {
+      const HNode& x = t.nodes[k];
+      Node& n = dn[k];
+      n.nI = (int)x.I.size();
+      n.nB = (int)x.B.size();
+      const long long f = n.nI + n.nB;
+      n.top = fac_base + fo;
+      n.bl = n.top + (long long)n.nI * f;
+      fo += (long long)n.nI * f + (long long)n.nB * n.nI;
+      n.par = d & 1;
+      n.s = so;
+      so += (long long)n.nB * n.nB;
+      n.fv = fv_base + vo;
+      vo += f;
+      flops += (double)n.nI * f * f;
+    }
+    L.fac_stride = fo;
+    L.s_stride = so;
+    L.fv_stride = vo;
+    for (int k : by_depth[d]) {
+      dn[k].fst = fo;
+      dn[k].sst = so;
+      dn[k].fvst = vo;
+    }
+    fac_base += fo * B;
+    fv_base += vo * B;
+    h->sar_elems[d & 1] = std::max(h->sar_elems[d & 1], (size_t)(so * B));
+  }
+  h->fac_elems = (size_t)fac_base;
+  h->fv_elems = (size_t)fv_base;
+  h->flops = flops * (double)B;
+  // cells, descriptors and child maps
+  const int di[5] = {0, -1, 1, 0, 0}, dj[5] = {0, 0, 0, -1, 1};
+  for (int k = 0; k < nn; ++k) {
+    const HNode& x = t.nodes[k];
+    Node& n = dn[k];
+    n.cells = (int)cells.size();
+    cells.insert(cells.end(), x.I.begin(), x.I.end());
+    cells.insert(cells.end(), x.B.begin(), x.B.end());
+    for (int q = 0; q < n.nI; ++q) pos[x.I[q]] = q;
+    for (int q = 0; q < n.nB; ++q) pos[x.B[q]] = n.nI + q;
+    n.desc = (int)desc.size();
+    for (int q = 0; q < n.nI; ++q) {
+      const int cell = x.I[q], i = cell / ny, j = cell % ny;
+      for (int dir = 0; dir < 5; ++dir) {
+        const int ii = i + di[dir], jj = j + dj[dir];
+        if (ii < 0 || ii >= nx || jj < 0 || jj >= ny) continue;  // no periodic wrap
+        const int p = pos[ii * ny + jj];
+        if (p >= 0) desc.push_back(Desc{q, p, cell, dir});
+      }
+    }
+    for (int q = 0; q < n.nB; ++q) {
+      const int cell = x.B[q], i = cell / ny, j = cell % ny;
+      for (int dir = 1; dir < 5; ++dir) {
+        const int ii = i + di[dir], jj = j + dj[dir];
+        if (ii < 0 || ii >= nx || jj < 0 || jj >= ny) continue;
+        const int p = pos[ii * ny + jj];
+        if (p >= 0 && p < n.nI) desc.push_back(Desc{n.nI + q, p, cell, dir});
+      }
+    }
+    n.ndesc = (int)desc.size() - n.desc;
+    for (int s = 0; s < 2; ++s) {
+      n.child[s] = x.child[s];
+      n.cmap[s] = -1;
+      if (x.child[s] < 0) continue;
+      n.cmap[s] = (int)cmap.size();
+      for (int cell : t.nodes[x.child[s]].B) {
+        const int p = pos[cell];
+        if (p < 0) {
+          set_error("nested dissection: a child's boundary cell is outside its parent's front");
+          return CEV_ERR_INVALID;
+        }
+        cmap.push_back(p);
+      }
+    }
+    for (int c : x.I) pos[c] = -1;
+    for (int c : x.B) pos[c] = -1;
+  }
+  // work lists per depth
+  for (int d = 0; d < h->ndepth; ++d) {
+    Level& L = h->levels[d];
+    for (int k : by_depth[d]) {
+      const Node& n = dn[k];
+      const int f = n.nI + n.nB;
+      L.max_f = std::max(L.max_f, f);
+      L.max_nI = std::max(L.max_nI, n.nI);
+      const int nch = (f + TILE - 1) / TILE;
+      if (f <= SMALL_F) {
+        L.small.push_back(k);
+        L.max_f_small = std::max(L.max_f_small, f);
+      } else {
+        L.large.push_back(k);
+        L.max_nI_large = std::max(L.max_nI_large, n.nI);
+        for (int s = 0; s < 2; ++s)
+          if (n.child[s] >= 0)
+            for (int r = 0; r < dn[n.child[s]].nB; ++r) L.ext[s].push_back(make_int2(k, r));
+        for (int c = 0; c < nch; ++c) L.panel.push_back(make_int2(k, c));
+        for (int c = 0; c < nch * nch; ++c) L.tiles.push_back(make_int2(k, c));
+        for (int c = 0; c < (n.nB + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.gemv.push_back(make_int2(k, c));
+      }
+      for (int c = 0; c < (n.nI + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.bwd.push_back(make_int2(k, c));
+    }
+    if (!upload_all) continue;
+    int rc;
+    if ((rc = upload(&L.d_small, L.small)) || (rc = upload(&L.d_large, L.large)) ||
+        (rc = upload(&L.d_ext[0], L.ext[0])) || (rc = upload(&L.d_ext[1], L.ext[1])) ||
+        (rc = upload(&L.d_panel, L.panel)) || (rc = upload(&L.d_tiles, L.tiles)) ||
+        (rc = upload(&L.d_gemv, L.gemv)) || (rc = upload(&L.d_bwd, L.bwd)))
+      return rc;
+  }
+  if (n_nodes) *n_nodes = dn.size();
+  if (n_desc) *n_desc = desc.size();
+  if (cover) {
+    // every cell eliminated exactly once: sum over nodes of the cell ids of I
+    // must equal 0 + 1 + ... + (n - 1), and the count must be n
+    long long sum = 0, cnt = 0;
+    for (const auto& x : t.nodes) {
+      cnt += (long long)x.I.size();
+      for (int c : x.I) sum += c;
+    }
+    const long long n = (long long)h->nx * h->ny;
+    cover[0] = cnt - n;
+    cover[1] = sum - n * (n - 1) / 2;
+  }
+  if (!upload_all) return CEV_OK;
+  int rc;
+  if ((rc = upload(&h->d_nodes, dn)) || (rc = upload(&h->d_cells, cells)) ||
+      (rc = upload(&h->d_cmap, cmap)) || (rc = upload(&h->d_desc, desc)))
+    return rc;
+  return CEV_OK;
+}
+
+static Args make_args(const cev_nd_precond_s* h, const Op& op) {
+  Args a;
+  a.op = op;
+  a.nodes = h->d_nodes;
+  a.cells = h->d_cells;
+  a.cmap = h->d_cmap;
+  a.desc = h->d_desc;
+  a.fac = h->fac;
+  a.sar[0] = h->sar[0];
+  a.sar[1] = h->sar[1];
+  a.fv = h->fv;
+  a.fault = h->fault;
+  a.n = h->n;
+  return a;
+}
+
+template <int FS, int TR, int TC>
+static int launch_small(const Args& a, const Level& L, int B, cudaStream_t s, int slot) {
+  const int bytes = (FS * FS + 2 * FS) * (int)sizeof(float2);
+  int rc = allow_smem((const void*)k_small<FS, TR, TC>, slot, bytes);
+  if (rc != CEV_OK) return rc;
+  k_small<FS, TR, TC><<<dim3((unsigned)L.small.size(), B), TR * TC, bytes, s>>>(a, L.d_small);
+  CEV_CHECK_LAUNCH("nd k_small");
+  return CEV_OK;
+}
+
+static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
+  const Args a = make_args(h, op);
+  const int B = h->batch;
+  CEV_CUDA(cudaMemsetAsync(h->fault, 0, sizeof(int), s));
+  long long fac_base = 0;
+  std::vector<long long> base(h->ndepth);
+  for (int d = 0; d < h->ndepth; ++d) {
+    base[d] = fac_base;
+    fac_base += h->levels[d].fac_stride * B;
+  }
+  for (int d = h->ndepth - 1; d >= 0; --d) {
+    const Level& L = h->levels[d];
+    if (!L.large.empty()) {
+      CEV_CUDA(cudaMemsetAsync(h->fac + base[d], 0, sizeof(float2) * L.fac_stride * B, s));
+      if (L.s_stride > 0)
+        CEV_CUDA(cudaMemsetAsync(h->sar[d & 1], 0, sizeof(float2) * L.s_stride * B, s));
+    }
+    if (!L.small.empty()) {
+      int rc;
+      if (L.max_f_small <= 32) rc = launch_small<32, 8, 16>(a, L, B, s, 0);
+      else if (L.max_f_small <= 64) rc = launch_small<64, 16, 16>(a, L, B, s, 1);
+      else rc = launch_small<128, 16, 32>(a, L, B, s, 2);
+      if (rc != CEV_OK) return rc;
+    }
+    if (L.large.empty()) continue;
+    const unsigned nl = (unsigned)L.large.size();
+    k_orig<<<dim3(nl, B), 256, 0, s>>>(a, L.d_large);
+    for (int sl = 0; sl < 2; ++sl)
+      if (!L.ext[sl].empty())
+        k_extend<<<dim3((unsigned)L.ext[sl].size(), B), 128, 0, s>>>(a, L.d_ext[sl], sl);
+    CEV_CHECK_LAUNCH("nd assemble");
+    for (int k0 = 0; k0 < L.max_nI_large; k0 += NB) {
+      k_pivblock<<<dim3(nl, B), 256, 0, s>>>(a, L.d_large, k0);
+      k_rowpanel<<<dim3((unsigned)L.panel.size(), B), 256, 0, s>>>(a, L.d_panel, k0);
+      k_update<<<dim3((unsigned)L.tiles.size(), B), 128, 0, s>>>(a, L.d_tiles, k0);
+      k_colpanel<<<dim3((unsigned)L.panel.size(), B), 256, 0, s>>>(a, L.d_panel, k0);
+    }
+    CEV_CHECK_LAUNCH("nd sweep");
+  }
+  return CEV_OK;
+}
+
+}  // namespace nd
+
+int nd_apply(cev_nd_precond_s* h, const float2* v, float2* z, const double* sc, int sc_stride,
+             int sc_index, const KState* st, cudaStream_t s) {
+  Op op{};  // entries are not needed by the apply kernels
+  const Args a = nd::make_args(h, op);
+  nd::ApplyIO io{v, z, sc, sc_stride, sc_index, st};
+  const int B = h->batch;
+  int rc;
+  for (int d = h->ndepth - 1; d >= 0; --d) {
+    const nd::Level& L = h->levels[d];
+    if (!L.small.empty()) {
+      const int bytes = L.max_f_small * (int)sizeof(float2);
+      nd::k_fwd<true><<<dim3((unsigned)L.small.size(), B), 256, bytes, s>>>(a, io, L.d_small);
+    }
+    if (!L.large.empty()) {
+      const int bytes = L.max_f * (int)sizeof(float2);
+      if ((rc = nd::allow_smem((const void*)nd::k_fwd<false>, 3, bytes)) != CEV_OK) return rc;
+      nd::k_fwd<false><<<dim3((unsigned)L.large.size(), B), 256, bytes, s>>>(a, io, L.d_large);
+      if (!L.gemv.empty()) {
+        const int gb = L.max_nI * (int)sizeof(float2);
+        if ((rc = nd::allow_smem((const void*)nd::k_fwd_gemv, 4, gb)) != CEV_OK) return rc;
+        nd::k_fwd_gemv<<<dim3((unsigned)L.gemv.size(), B), 256, gb, s>>>(a, io, L.d_gemv);
+      }
+    }
+    CEV_CHECK_LAUNCH("nd forward");
+  }
+  for (int d = 0; d < h->ndepth; ++d) {
+    const nd::Level& L = h->levels[d];
+    if (L.bwd.empty()) continue;
+    const int bytes = L.max_f * (int)sizeof(float2);
+    if ((rc = nd::allow_smem((const void*)nd::k_bwd, 5, bytes)) != CEV_OK) return rc;
+    nd::k_bwd<<<dim3((unsigned)L.bwd.size(), B), 256, bytes, s>>>(a, io, L.d_bwd);
+    CEV_CHECK_LAUNCH("nd backward");
+  }
+  return CEV_OK;
+}
+
+int nd_check(const cev_nd_precond_s* h, const cev_fdfd_plan_s* p, int kind, int transpose) {
+  CEV_REQUIRE(h != nullptr, "the direct preconditioner needs opts.direct");
+  CEV_REQUIRE(h->plan == p, "direct preconditioner built for another plan");
+  CEV_REQUIRE(h->transpose == transpose,
+              "direct preconditioner built for transpose=%d, solve has transpose=%d", h->transpose,
+              transpose);
+  if (kind == CEV_PRECOND_DIRECT)
+    CEV_REQUIRE(h->shift == 0.0, "CEV_PRECOND_DIRECT needs a factorisation with shift 0 (got %g)",
+                h->shift);
+  else
+    CEV_REQUIRE(h->shift != 0.0,
+                "CEV_PRECOND_SHIFTED_LAPLACIAN needs a factorisation with a non-zero shift");
+  return CEV_OK;
+}
+
+}  // namespace cev
+
+extern "C" {
+
+int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double* eps,
+                          int eps_shared, int transpose, double shift, cudaStream_t stream) {
+  CEV_REQUIRE(out != nullptr && plan != nullptr && eps != nullptr, "NULL argument");
+  *out = nullptr;
+  CEV_REQUIRE(plan->mf_nsb < 0, "multi-frequency plans have no direct preconditioner");
+  CEV_REQUIRE(plan->nx >= 2 && plan->ny >= 2, "direct preconditioner needs nx, ny >= 2");
+  CEV_REQUIRE((size_t)plan->nx * plan->ny < ((size_t)1 << 31), "grid too large");
+  CEV_REQUIRE(std::isfinite(shift) && shift >= 0.0, "shift must be finite and >= 0");
+  auto* h = new cev_nd_precond_s();
+  h->nx = plan->nx;
+  h->ny = plan->ny;
+  h->batch = plan->batch;
+  h->pol = plan->pol;
+  h->transpose = transpose ? 1 : 0;
+  h->shift = shift;
+  h->n = plan->n();
+  h->plan = plan;
+  cudaGetDevice(&h->device);
+  int rc = nd::analyse(h, true);
+  auto fail = [&](int code) {
+    delete h;
+    return code;
+  };
+  if (rc != CEV_OK) return fail(rc);
+  auto alloc = [&](float2** p, size_t elems) -> int {
+    if (elems == 0) return CEV_OK;
+    const cudaError_t e = cudaMalloc((void**)p, sizeof(float2) * elems);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error("direct preconditioner: cannot allocate %zu bytes on the device",
+                sizeof(float2) * elems);
+      return CEV_ERR_CUDA;
+    }
+    return CEV_OK;
+  };
+  if ((rc = alloc(&h->fac, h->fac_elems)) || (rc = alloc(&h->sar[0], h->sar_elems[0])) ||
+      (rc = alloc(&h->sar[1], h->sar_elems[1])) || (rc = alloc(&h->fv, h->fv_elems)))
+    return fail(rc);
+  if (cudaMalloc((void**)&h->fault, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("direct preconditioner: cannot allocate its fault flag");
+    return fail(CEV_ERR_CUDA);
+  }
+  const int tr = h->transpose;
+  nd::Op op{plan->pol, plan->nx, plan->ny, plan->eps_complex,
+            eps_shared ? (size_t)0 : plan->n(), eps, plan->cx32[tr], plan->cy32[tr],
+            plan->k2_32, (float)shift};
+  if ((rc = nd::factor(h, op, stream)) != CEV_OK) return fail(rc);
+  // the Schur arenas are only needed during the factorisation
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return fail(cuda_status(e, "direct preconditioner factorisation"));
+  int fault = 0;
+  cudaMemcpy(&fault, h->fault, sizeof(int), cudaMemcpyDeviceToHost);
+  if (fault) {
+    set_error("direct preconditioner: a zero or non-finite pivot in the complex64 factorisation");
+    return fail(CEV_ERR_NUMERIC);
+  }
+  cudaFree(h->sar[0]);
+  cudaFree(h->sar[1]);
+  h->sar[0] = h->sar[1] = nullptr;
+  *out = h;
+  return CEV_OK;
+}
+
+int cev_nd_precond_apply(cev_nd_precond h, const void* v, void* z, cudaStream_t stream) {
+  CEV_REQUIRE(h != nullptr && v != nullptr && z != nullptr, "NULL argument");
+  return nd_apply(h, (const float2*)v, (float2*)z, nullptr, 0, 0, nullptr, stream);
+}
+
+int cev_nd_precond_info(cev_nd_precond h, size_t* factor_bytes, double* factor_cmacs,
+                        int* depths) {
+  CEV_REQUIRE(h != nullptr, "NULL handle");
+  if (factor_bytes) *factor_bytes = sizeof(float2) * h->fac_elems;
+  if (factor_cmacs) *factor_cmacs = h->flops;
+  if (depths) *depths = h->ndepth;
+  return CEV_OK;
+}
+
+int cev_nd_analyse(int nx, int ny, size_t* n_nodes, int* depths, size_t* factor_elems,
+                   double* factor_cmacs, size_t* n_desc, long long* cover) {
+  CEV_REQUIRE(nx >= 2 && ny >= 2 && (size_t)nx * ny < ((size_t)1 << 31), "bad grid %d x %d", nx,
+              ny);
+  cev_nd_precond_s h;
+  h.nx = nx;
+  h.ny = ny;
+  h.batch = 1;
+  h.n = (size_t)nx * ny;
+  long long cv[2] = {0, 0};
+  const int rc = nd::analyse(&h, false, n_nodes, n_desc, cv);
+  if (rc != CEV_OK) return rc;
+  if (depths) *depths = h.ndepth;
+  if (factor_elems) *factor_elems = h.fac_elems;
+  if (factor_cmacs) *factor_cmacs = h.flops;
+  if (cover) {
+    cover[0] = cv[0];
+    cover[1] = cv[1];
+  }
+  return CEV_OK;
+}
+
+int cev_nd_precond_destroy(cev_nd_precond h) {
+  delete h;
+  return CEV_OK;
+}
+
+}  // extern "C"

@@ -65,6 +65,13 @@ int precond_setup(Precond& pc, const cev_fdfd_plan_s* p, const cev_solve_opts& o
     pc.impl = &ls;
     return CEV_OK;
   }
+  if (o.precond == CEV_PRECOND_DIRECT || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN) {
+    auto* h = (cev_nd_precond_s*)o.direct;
+    const int rc = nd_check(h, p, o.precond, o.transpose ? 1 : 0);
+    if (rc != CEV_OK) return rc;
+    pc.impl = h;
+    return CEV_OK;
+  }
   CEV_REQUIRE(o.precond == CEV_PRECOND_SEPARABLE, "preconditioner %d is not available", o.precond);
   auto* h = (cev_sep_precond_s*)o.separable;
   CEV_REQUIRE(h != nullptr, "CEV_PRECOND_SEPARABLE needs opts.separable");
@@ -116,6 +123,8 @@ int precond_apply(Precond& pc, const KCtx& c, int j, int m, const float2* v, flo
     const LearnedState& ls = *(const LearnedState*)pc.impl;
     return nn::learned_forward(ls.h, ls.p, ls.eps, ls.eps_shared, v, z, c.sc, m + 1, j, s);
   }
+  if (pc.kind == CEV_PRECOND_DIRECT || pc.kind == CEV_PRECOND_SHIFTED_LAPLACIAN)
+    return nd_apply((cev_nd_precond_s*)pc.impl, v, z, c.sc, m + 1, j, c.st, s);
   CEV_REQUIRE(pc.kind == CEV_PRECOND_SEPARABLE, "no preconditioner configured");
   SepState& st = *(SepState*)pc.impl;
   cev_sep_precond_s& h = *st.h;

@@ -23,6 +23,9 @@ _DEFAULT_OPTS = dict(tol=1e-6, inner_rtol=1e-4, max_iters=20000, restart=30, pre
                      reorth=0, max_stall=20, mg_levels=0, mg_shift=0.5, sep_shift=0.0)
 
 
+_last_info = None  # infos of the latest solve (read by fdfd.solve as last_info)
+
+
 class SolverWarning(UserWarning):
     """A solve finished without reaching its tolerance."""
 
@@ -140,7 +143,7 @@ def make_opts(**kw):
     for k, v in kw.items():
         if v is None:
             continue
-        if k not in o and k not in ("transpose", "use_x0", "learned", "separable"):
+        if k not in o and k not in ("transpose", "use_x0", "learned", "separable", "direct"):
             raise TypeError(f"unknown solver option {k!r}")
         o[k] = v
     s = _lib.SolveOpts()
@@ -160,6 +163,8 @@ def make_opts(**kw):
     s.learned = None if lp is None else C.c_void_p(lp.handle_ptr())
     sp = o.get("separable")
     s.separable = None if sp is None else sp.handle
+    dp = o.get("direct")
+    s.direct = None if dp is None else dp.handle
     return s
 
 
@@ -177,6 +182,12 @@ def solve(plan, eps, b, transpose=False, x0=None, strict=False, fallback=True, *
     """Solve A x = b (A^T x = b) for every problem; b complex (batch, nx, ny) in SI units.
 
     Returns (x complex128, infos).  Non-convergence warns (or raises with strict).
+    ``precond="direct"`` preconditions with complex64 nested-dissection
+    factors of the operator (``DirectPrecond``, cached per plan and eps), the
+    GPU counterpart of the sparse LU behind ceviche's solve; it converges in a
+    few iterations where plain GMRES needs thousands.
+    ``precond="shifted_laplacian"`` uses the same factorisation of the
+    shifted operator (mass term times 1 - i*mg_shift).
     With a preconditioner (``precond`` "learned" or "separable") and
     ``fallback``, a solve that stops short of ``tol`` (stagnation of the
     flexible GMRES) continues with plain GMRES from its iterate for the rest of
@@ -186,11 +197,13 @@ def solve(plan, eps, b, transpose=False, x0=None, strict=False, fallback=True, *
     the network for the first cycles, plain GMRES after); the plain phase
     keeps at least the default stall limit.
     """
+    global _last_info
     x, res, rc, tol = _solve_once(plan, eps, b, transpose, x0, **opts)
     if rc > 0 and fallback and opts.get("precond", "none") not in ("none", 0):
         left = int(opts.get("max_iters", _DEFAULT_OPTS["max_iters"])) - max(r["iterations"] for r in res)
         if left > 0:
-            plain = {k: v for k, v in opts.items() if k not in ("precond", "learned", "separable")}
+            plain = {k: v for k, v in opts.items()
+                     if k not in ("precond", "learned", "separable", "direct")}
             plain["max_iters"] = left
             # the stall limit decides when to leave the preconditioned phase; the
             # plain phase keeps at least the default patience
@@ -209,6 +222,7 @@ def solve(plan, eps, b, transpose=False, x0=None, strict=False, fallback=True, *
         if strict:
             raise _lib.CevError(msg)
         warnings.warn(msg, SolverWarning, stacklevel=2)
+    _last_info = res
     return x, res
 
 
@@ -222,6 +236,10 @@ def _solve_once(plan, eps, b, transpose, x0, **opts):
         keep = SeparablePrecond(plan, e, shift=opts.get("sep_shift", 0.0), transpose=transpose)
         opts = dict(opts, separable=keep)
         e, sh = _eps_arg(plan, eps, torch.float64)  # re-assert the eps kind on the plan
+    if opts.get("precond") in ("direct", "shifted_laplacian") and opts.get("direct") is None:
+        shift = 0.0 if opts["precond"] == "direct" else float(opts.get("mg_shift", 0.5))
+        keep = direct_precond(plan, e, transpose=transpose, shift=shift)
+        opts = dict(opts, direct=keep)
     s = make_opts(transpose=transpose, use_x0=x0 is not None, **opts)
     if x0 is not None:
         x = _field_arg(plan, x0, torch.complex128).clone()
@@ -360,6 +378,56 @@ class SeparablePrecond:
         if h is not None and getattr(_lib, "_lib", None) is not None:
             _lib._lib.cev_sep_precond_destroy(h)
             self.handle = None
+
+
+class DirectPrecond:
+    """cev_nd_precond for a plan and an eps: complex64 nested-dissection
+    factors of the plan's operator (A or A^T), or of the shifted operator with
+    ``shift`` > 0.  The factorisation runs on the GPU when the object is made;
+    ``factor_bytes`` and ``factor_cmacs`` report its size and work."""
+
+    def __init__(self, plan, eps, transpose=False, shift=0.0):
+        lib = _lib.load()
+        e, sh = _eps_arg(plan, eps, torch.float64)
+        h = C.c_void_p()
+        check(lib.cev_nd_precond_create(C.byref(h), plan.handle, ptr(e), sh, int(bool(transpose)),
+                                        float(shift), stream_ptr()), "nd_precond_create")
+        self.handle = h
+        self.plan = plan  # the handle reads the plan's tables; keep it alive
+        nb, fl, nd = C.c_size_t(), C.c_double(), C.c_int()
+        check(lib.cev_nd_precond_info(h, C.byref(nb), C.byref(fl), C.byref(nd)), "nd_precond_info")
+        self.factor_bytes, self.factor_cmacs, self.depths = nb.value, fl.value, nd.value
+        self.transpose, self.shift = bool(transpose), float(shift)
+
+    def apply(self, v):
+        """z = M^-1 v for complex64 (batch, nx, ny) device tensors."""
+        vt = _field_arg(self.plan, v, torch.complex64)
+        z = torch.empty_like(vt)
+        check(_lib.load().cev_nd_precond_apply(self.handle, ptr(vt), ptr(z), stream_ptr()),
+              "nd_precond_apply")
+        return z
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and getattr(_lib, "_lib", None) is not None:
+            _lib._lib.cev_nd_precond_destroy(h)
+            self.handle = None
+
+
+def direct_precond(plan, eps, transpose=False, shift=0.0):
+    """The DirectPrecond of (plan, eps, transpose, shift), reused while eps is
+    unchanged (one factorisation kept per plan, transpose flag and shift)."""
+    cache = plan.__dict__.setdefault("_nd_cache", {})
+    key = (bool(transpose), float(shift))
+    hit = cache.get(key)
+    e = eps.detach()
+    if hit is not None and hit[0].shape == e.shape and hit[0].dtype == e.dtype \
+            and torch.equal(hit[0], e):
+        return hit[1]
+    cache.pop(key, None)  # free the old factors before making new ones
+    dp = DirectPrecond(plan, e, transpose=transpose, shift=shift)
+    cache[key] = (e.clone(), dp)
+    return dp
 
 
 class FDFDSolve(torch.autograd.Function):

@@ -48,9 +48,10 @@ extern "C" {
 #define CEV_PREC_C128 1 /* complex128 fields, double eps */
 
 #define CEV_PRECOND_NONE 0
-#define CEV_PRECOND_SHIFTED_LAPLACIAN 1
+#define CEV_PRECOND_SHIFTED_LAPLACIAN 1 /* nested-dissection factors of the shifted operator */
 #define CEV_PRECOND_LEARNED 2
 #define CEV_PRECOND_SEPARABLE 3 /* exact inverse of the constant-eps stretched operator */
+#define CEV_PRECOND_DIRECT 4    /* nested-dissection complex64 factors of the operator */
 
 /* Last error message of the calling thread ("" if none). */
 CEV_API const char* cev_last_error_string(void);
@@ -112,10 +113,11 @@ typedef struct {
   int use_x0;         /* x holds an initial guess on entry */
   int reorth;         /* 1: classical Gram-Schmidt with a second pass */
   int max_stall;      /* cycles without a 10% residual drop before CEV_STAGNATED */
-  int mg_levels;      /* shifted-Laplacian preconditioner: multigrid levels (0 = auto) */
-  double mg_shift;    /* shifted-Laplacian imaginary shift beta (default 0.5) */
+  int mg_levels;      /* reserved (0) */
+  double mg_shift;    /* shifted-operator imaginary shift beta the caller factors with (0.5) */
   const void* learned; /* CEV_PRECOND_LEARNED: a cev_learned_precond handle */
   const void* separable; /* CEV_PRECOND_SEPARABLE: a cev_sep_precond handle */
+  const void* direct;  /* CEV_PRECOND_DIRECT / _SHIFTED_LAPLACIAN: a cev_nd_precond handle */
 } cev_solve_opts;
 
 typedef struct {
@@ -149,6 +151,41 @@ CEV_API int cev_sep_precond_create(cev_sep_precond* out, cev_fdfd_plan plan, int
                                    const void* vx, const void* vxi, const void* vy,
                                    const void* vyi, const void* dinv);
 CEV_API int cev_sep_precond_destroy(cev_sep_precond h);
+
+/*
+ * Direct preconditioner (CEV_PRECOND_DIRECT): a nested-dissection multifrontal
+ * factorisation of the plan's non-dimensional operator A' (or A'^T with
+ * transpose = 1) for eps (double [1 or batch][nx][ny], real or, with
+ * cev_fdfd_plan_set_eps_complex, complex), in complex64 without pivoting and
+ * without the periodic wrap entries.  It stands where ceviche factors the
+ * assembled matrix with SuperLU (ceviche/solvers.py:50-62, reached from
+ * primitives.py:103-119); here the factors precondition flexible GMRES and the
+ * FP64 true residual still decides convergence, so the complex64 rounding and
+ * the dropped wrap only cost iterations.  The separators split the longer
+ * side of each box; fronts are dense and swept by Gauss-Jordan, so applying
+ * M^-1 is GEMVs.  shift > 0 factors the shifted operator (mass term times
+ * 1 - i*shift), the exact complex-shifted-Laplacian inverse that
+ * CEV_PRECOND_SHIFTED_LAPLACIAN uses.  The handle owns its factors (about
+ * 80-110 complex64 numbers per cell and problem; cev_nd_precond_info) and
+ * keeps a pointer to the plan, which must outlive it.  create synchronises
+ * the stream; it returns CEV_ERR_NUMERIC for a zero pivot.
+ * apply: z = M^-1 v for every problem (complex64 [batch][nx][ny]).
+ */
+typedef struct cev_nd_precond_s* cev_nd_precond;
+CEV_API int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double* eps,
+                                  int eps_shared, int transpose, double shift,
+                                  cudaStream_t stream);
+CEV_API int cev_nd_precond_apply(cev_nd_precond h, const void* v, void* z, cudaStream_t stream);
+CEV_API int cev_nd_precond_info(cev_nd_precond h, size_t* factor_bytes, double* factor_cmacs,
+                                int* depths);
+CEV_API int cev_nd_precond_destroy(cev_nd_precond h);
+/* Host-side analysis of the nested-dissection tree of an nx x ny grid (no
+ * CUDA call): tree nodes, depths, complex64 factor entries and Gauss-Jordan
+ * complex multiply-adds per problem, original-entry count, and cover[2] =
+ * (cells eliminated - nx*ny, sum of their ids - sum of 0..nx*ny-1), both 0
+ * when every cell is eliminated exactly once. */
+CEV_API int cev_nd_analyse(int nx, int ny, size_t* n_nodes, int* depths, size_t* factor_elems,
+                           double* factor_cmacs, size_t* n_desc, long long* cover);
 
 /*
  * Learned preconditioner (CEV_PRECOND_LEARNED).  A 4-level convolutional
