@@ -91,6 +91,10 @@ __device__ __forceinline__ float warp_sumf(float v) {
 
 // Number of SMs of the current device (cached per device).
 int sm_count();
+// Allows `bytes` of dynamic shared memory for kernel `fn` on the current
+// device (set once per device and kernel; thread-safe), and with carveout >= 0
+// the preferred shared-memory carve-out in percent.
+int allow_dynamic_smem(const void* fn, int bytes, int carveout = -1);
 
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 

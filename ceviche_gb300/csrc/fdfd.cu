@@ -1,8 +1,11 @@
 // FDFD plan, matrix-free operator, field conversions and eps gradients.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "fdfd_plan.hpp"
 
@@ -24,17 +27,36 @@ int cuda_status(cudaError_t e, const char* where) {
 }
 
 int sm_count() {
-  static int cache[64] = {0};
+  static std::atomic<int> cache[64];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
-  if (cache[dev] == 0) {
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v == 0) {
     int n = 0;
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
       n = 148;
-    cache[dev] = n;
+    cache[dev].store(n, std::memory_order_relaxed);
+    v = n;
   }
-  return cache[dev];
+  return v;
+}
+
+// The dynamic shared-memory limit is an attribute of a kernel on the current
+// device: record, per (device, kernel), the largest size already allowed.
+int allow_dynamic_smem(const void* fn, int bytes, int carveout) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> done;
+  int dev = 0;
+  CEV_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  int& have = done[std::make_pair(dev, fn)];
+  if (have >= bytes) return CEV_OK;
+  CEV_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  if (carveout >= 0)
+    CEV_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carveout));
+  have = bytes;
+  return CEV_OK;
 }
 
 // ------------------------------------------------------------ PML profiles

@@ -45,6 +45,14 @@ struct cev_fdtd_plan_s {
   void* iexx = nullptr;
   void* ieyy = nullptr;
   void* shadow = nullptr;  // second TM state for the time-blocked run (6 N R)
+  // Device pointers borrowed from elsewhere (the allocation-free runner's
+  // static scratch): run_tm_impl then never allocates, and nothing frees them
+  // (cev_fdtd_plan_destroy is never called on such a plan).
+  bool borrowed = false;
+  // persistent runner: neighbour lists of its tile grid, tile flags, fault word
+  int pcfg = -1, ptiles = 0;
+  int* pnbr = nullptr;
+  int* pflags = nullptr;  // [ptiles] flags, then the fault word
   std::vector<double> aHx, aDx, aHy, aDy;
   size_t n() const { return (size_t)nx * ny; }
   size_t rs() const { return prec == CEV_PREC_C128 ? sizeof(double) : sizeof(float); }
@@ -286,7 +294,25 @@ struct TBArgs {
   const int* probe_idx;
   R* probe_out;   // [t][np]
   R* dz_hist;     // HIST kernels: Dz after step t0+st goes to dz_hist[(t0+st+1)*N]
+  // PERSIST kernels: the whole run in one launch (see k_tm_tile)
+  int nsteps;           // steps of the run
+  R* xb[2][6];          // exchange buffers (hx, hy, dz, icex, icey, idz); block m uses xb[m & 1]
+  int* flags;           // [tiles] blocks published by each tile (zeroed before the launch)
+  const int* nbr;       // [tiles][NBR_MAX] tiles this tile exchanges with (-1 ends a list)
+  int* fault;           // set when a neighbour wait ran out
 };
+
+// Most tiles one persistent tile exchanges its ring with.
+constexpr int NBR_MAX = 16;
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 template <typename R, int TI, int TJ, int K, int NT>
 struct Tile {
@@ -298,7 +324,14 @@ struct Tile {
       7 * (size_t)RN * sizeof(R) + 5 * (size_t)(RI + RJ) * sizeof(R) + (size_t)K * sizeof(R);
 };
 
-template <typename R, int TI, int TJ, int K, int NT, bool HIST = false>
+// PERSIST: one cooperative launch runs all a.nsteps steps.  Each CTA keeps its
+// region resident; after every block of K steps its interior is exact and its
+// K-wide ring is stale, so it publishes its interior to the exchange buffer
+// xb[m & 1], releases flags[tile] = m + 1, waits (bounded) until every tile of
+// its neighbour list has published block m, and reloads the ring from the same
+// buffer.  Neighbour lists are symmetric, so a tile two blocks ahead can never
+// overwrite a buffer a neighbour is still reading.
+template <typename R, int TI, int TJ, int K, int NT, bool HIST = false, bool PERSIST = false>
 __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
   using T = Tile<R, TI, TJ, K, NT>;
   constexpr int RI = T::RI, RJ = T::RJ, RN = T::RN, CPT = T::CPT;
@@ -338,7 +371,8 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
     yf1[q] = c.f1H; yf2[q] = c.f2H; yg3[q] = R(2) * c.aH; yaD[q] = c.aD; ypD[q] = c.pD;
     pl |= (c.aH != R(0)) | (c.aD != R(0));
   }
-  for (int st = tid; st < nst; st += NT) sAmp[st] = a.ns > 0 ? a.amps[a.t0 + st] : R(0);
+  if (!PERSIST)
+    for (int st = tid; st < nst; st += NT) sAmp[st] = a.ns > 0 ? a.amps[a.t0 + st] : R(0);
   for (int q = tid; q < RN; q += NT) sW[q] = R(0);
   const bool pml = __syncthreads_or(pl);
   for (int k = tid; k < a.ns; k += NT) {
@@ -410,7 +444,44 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
       dm4[k] = R(-4) * ax * ay * pd;
     }
   }
-  for (int st = 0; st < nst; ++st) {
+  // interior cells owned by this tile (inside the grid) -> 6 field arrays
+  auto publish = [&](R* const* o) {
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+      const int q = tid + k * NT;
+      if (q < RN) {
+        const int r = q / RJ, c = q - r * RJ;
+        const int ii = gi0 + r, jj = gj0 + c;
+        if (r >= K && r < K + TI && c >= K && c < K + TJ && ii < a.nx && jj < a.ny) {
+          const size_t n = (size_t)ii * a.ny + jj;
+          o[0][n] = hx[k];
+          o[1][n] = hy[k];
+          o[2][n] = dz[k];
+          if (pml) {
+            if constexpr (REG_INT) {
+              o[3][n] = ixr[k];
+              o[4][n] = iyr[k];
+              o[5][n] = idr[k];
+            } else {
+              o[3][n] = sIx[q];
+              o[4][n] = sIy[q];
+              o[5][n] = sId[q];
+            }
+          }
+        }
+      }
+    }
+  };
+  const int nblk = PERSIST ? (a.nsteps + K - 1) / K : 1;
+  const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+  for (int blk = 0; blk < nblk; ++blk) {
+  const int t0 = PERSIST ? blk * K : a.t0;
+  const int bst = PERSIST ? min(K, a.nsteps - t0) : nst;
+  if (PERSIST) {
+    for (int st = tid; st < bst; st += NT) sAmp[st] = a.ns > 0 ? a.amps[t0 + st] : R(0);
+    __syncthreads();
+  }
+  for (int st = 0; st < bst; ++st) {
     const R amp = sAmp[st];
     if (!pml) {
       // no PML cell in the region: a = 0, so f1 = 1, f2 = S, mDz1 = 1,
@@ -538,34 +609,73 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
       const int ii = n / a.ny, jj = n - ii * a.ny;
       const int r = ii - gi0, c = jj - gj0;
       if (r >= K && r < K + TI && c >= K && c < K + TJ)
-        a.probe_out[(size_t)(a.t0 + st) * a.np + k] = sEz[r * RJ + c];
+        a.probe_out[(size_t)(t0 + st) * a.np + k] = sEz[r * RJ + c];
     }
   }
-  // write back the tile interior
-#pragma unroll
-  for (int k = 0; k < CPT; ++k) {
-    const int q = tid + k * NT;
-    if (q < RN) {
-      const int r = q / RJ, c = q - r * RJ;
-      const int ii = gi0 + r, jj = gj0 + c;
-      if (r >= K && r < K + TI && c >= K && c < K + TJ && ii < a.nx && jj < a.ny) {
-        const size_t n = (size_t)ii * a.ny + jj;
-        a.hx_o[n] = hx[k];
-        a.hy_o[n] = hy[k];
-        a.dz_o[n] = dz[k];
-        if (pml) {
-          if constexpr (REG_INT) {
-            a.icex_o[n] = ixr[k];
-            a.icey_o[n] = iyr[k];
-            a.idz_o[n] = idr[k];
-          } else {
-            a.icex_o[n] = sIx[q];
-            a.icey_o[n] = sIy[q];
-            a.idz_o[n] = sId[q];
+  if constexpr (PERSIST) {
+    if (blk + 1 < nblk) {
+      R* const* xb = a.xb[blk & 1];
+      publish(xb);
+      __syncthreads();
+      if (tid == 0) {
+        __threadfence();
+        st_release_gpu(a.flags + tile, blk + 1);
+      }
+      // bounded wait for the neighbours' block: about a second at most
+      bool late = false;
+      if (tid < NBR_MAX) {
+        const int nb = a.nbr[tile * NBR_MAX + tid];
+        if (nb >= 0) {
+          int spins = 0;
+          while (ld_acquire_gpu(a.flags + nb) < blk + 1) {
+            if (++spins > (1 << 22) || ld_acquire_gpu(a.fault) != 0) {
+              late = true;
+              break;
+            }
+            __nanosleep(128);
           }
         }
       }
+      if (__syncthreads_or(late)) {
+        if (tid == 0) atomicExch(a.fault, 1);
+        return;
+      }
+      // ring cells: the neighbours' published values (through L2)
+#pragma unroll
+      for (int k = 0; k < CPT; ++k) {
+        const int q = tid + k * NT;
+        if (q < RN) {
+          const int r = q / RJ, c = q - r * RJ;
+          if (!(r >= K && r < K + TI && c >= K && c < K + TJ)) {
+            const size_t n = (size_t)gi(r) * a.ny + gj(c);
+            hx[k] = __ldcg(xb[0] + n);
+            hy[k] = __ldcg(xb[1] + n);
+            dz[k] = __ldcg(xb[2] + n);
+            if (pml) {
+              if constexpr (REG_INT) {
+                ixr[k] = __ldcg(xb[3] + n);
+                iyr[k] = __ldcg(xb[4] + n);
+                idr[k] = __ldcg(xb[5] + n);
+              } else {
+                sIx[q] = __ldcg(xb[3] + n);
+                sIy[q] = __ldcg(xb[4] + n);
+                sId[q] = __ldcg(xb[5] + n);
+              }
+            }
+            sEz[q] = dz[k] * ie[k];
+          }
+        }
+      }
+      __syncthreads();
     }
+  }
+  }  // blocks of K steps
+  // write back the tile interior
+  if constexpr (PERSIST) {
+    publish(a.xb[(nblk - 1) & 1]);
+  } else {
+    R* const o[6] = {a.hx_o, a.hy_o, a.dz_o, a.icex_o, a.icey_o, a.idz_o};
+    publish(o);
   }
 }
 
@@ -582,9 +692,7 @@ struct TileLauncher {
   static constexpr TileCfg c = TILE_CFGS[I];
   using T = Tile<R, c.ti, c.tj, c.k, c.nt>;
   static int prepare() {
-    CEV_CUDA(cudaFuncSetAttribute(k_tm_tile<R, c.ti, c.tj, c.k, c.nt>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem));
-    return CEV_OK;
+    return allow_dynamic_smem((const void*)k_tm_tile<R, c.ti, c.tj, c.k, c.nt>, (int)T::smem);
   }
   static void launch(dim3 g, const TBArgs<R>& a, cudaStream_t s) {
     k_tm_tile<R, c.ti, c.tj, c.k, c.nt><<<g, c.nt, T::smem, s>>>(a);
@@ -830,13 +938,116 @@ template <typename R>
 static int hist_launch(bool prepare, dim3 g, const TBArgs<R>& a, cudaStream_t s) {
   constexpr TileCfg c = TILE_CFGS[HIST_CFG];
   using T = Tile<R, c.ti, c.tj, c.k, c.nt>;
-  if (prepare) {
-    CEV_CUDA(cudaFuncSetAttribute(k_tm_tile<R, c.ti, c.tj, c.k, c.nt, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::smem));
-    return CEV_OK;
-  }
+  if (prepare)
+    return allow_dynamic_smem((const void*)k_tm_tile<R, c.ti, c.tj, c.k, c.nt, true>, (int)T::smem);
   k_tm_tile<R, c.ti, c.tj, c.k, c.nt, true><<<g, c.nt, T::smem, s>>>(a);
   return CEV_OK;
+}
+
+// ------------------------------------------------ persistent TM runner
+// Tile shapes of the single-launch runner: every tile's CTA must be resident
+// at once (cooperative launch), so the runner serves grids whose tile count
+// fits the GPU (about 600 x 600 cells); larger grids take the launch-per-K
+// path, where launch overhead is a small share.
+constexpr TileCfg PERSIST_CFGS[] = {{34, 34, 8, 512}, {42, 42, 8, 512}, {50, 50, 8, 512},
+                                    {34, 34, 4, 512}};
+constexpr int N_PERSIST_CFGS = sizeof(PERSIST_CFGS) / sizeof(PERSIST_CFGS[0]);
+
+template <typename R, int I>
+struct PersistLauncher {
+  static constexpr TileCfg c = PERSIST_CFGS[I];
+  using T = Tile<R, c.ti, c.tj, c.k, c.nt>;
+  static const void* fn() { return (const void*)k_tm_tile<R, c.ti, c.tj, c.k, c.nt, false, true>; }
+  static int capacity() {
+    if (T::smem > 227 * 1024 || allow_dynamic_smem(fn(), (int)T::smem) != CEV_OK) {
+      cudaGetLastError();
+      return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tm_tile<R, c.ti, c.tj, c.k, c.nt, false, true>,
+                                                      c.nt, T::smem) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    return n * sm_count();
+  }
+  static int launch(dim3 g, TBArgs<R>& a, cudaStream_t s) {
+    void* args[] = {&a};
+    CEV_CUDA(cudaLaunchCooperativeKernel(fn(), g, dim3(c.nt), args, T::smem, s));
+    return CEV_OK;
+  }
+};
+
+template <typename R, int I = 0>
+static int persist_capacity(int cfg) {
+  if constexpr (I < N_PERSIST_CFGS) {
+    return cfg == I ? PersistLauncher<R, I>::capacity() : persist_capacity<R, I + 1>(cfg);
+  } else {
+    return 0;
+  }
+}
+
+template <typename R, int I = 0>
+static int persist_launch(int cfg, dim3 g, TBArgs<R>& a, cudaStream_t s) {
+  if constexpr (I < N_PERSIST_CFGS) {
+    return cfg == I ? PersistLauncher<R, I>::launch(g, a, s) : persist_launch<R, I + 1>(cfg, g, a, s);
+  } else {
+    set_error("bad persistent tile configuration %d", cfg);
+    return CEV_ERR_INVALID;
+  }
+}
+
+// Symmetric neighbour lists of the tile grid: tile T exchanges with the owner
+// of every ring cell of its region, and the owner with T.  Returns false when
+// some tile has more than NBR_MAX neighbours.
+static bool persist_neighbours(int nx, int ny, const TileCfg& c, std::vector<int>& out) {
+  const int gy = (nx + c.ti - 1) / c.ti, gx = (ny + c.tj - 1) / c.tj, tiles = gx * gy;
+  const int RI = c.ti + 2 * c.k, RJ = c.tj + 2 * c.k;
+  std::vector<std::vector<int>> nb(tiles);
+  auto add = [&](int a, int b) {
+    if (std::find(nb[a].begin(), nb[a].end(), b) == nb[a].end()) nb[a].push_back(b);
+  };
+  for (int ty = 0; ty < gy; ++ty)
+    for (int tx = 0; tx < gx; ++tx) {
+      const int t = ty * gx + tx, gi0 = ty * c.ti - c.k, gj0 = tx * c.tj - c.k;
+      for (int r = 0; r < RI; ++r)
+        for (int q = 0; q < RJ; ++q) {
+          if (r >= c.k && r < c.k + c.ti && q >= c.k && q < c.k + c.tj) continue;
+          const int i = ((gi0 + r) % nx + nx) % nx, j = ((gj0 + q) % ny + ny) % ny;
+          const int o = (i / c.ti) * gx + (j / c.tj);
+          if (o == t) continue;
+          add(t, o);
+          add(o, t);
+        }
+    }
+  out.assign((size_t)tiles * NBR_MAX, -1);
+  for (int t = 0; t < tiles; ++t) {
+    if ((int)nb[t].size() > NBR_MAX) return false;
+    for (size_t k = 0; k < nb[t].size(); ++k) out[(size_t)t * NBR_MAX + k] = nb[t][k];
+  }
+  return true;
+}
+
+// Persistent configuration for this grid, or -1.  CEV_FDTD_PERSIST=0 turns
+// the runner off; CEV_FDTD_PERSIST=<i+1> forces configuration i.
+template <typename R>
+static int pick_persist(int nx, int ny) {
+  const char* e = std::getenv("CEV_FDTD_PERSIST");
+  int forced = -1;
+  if (std::getenv("CEV_FDTD_TILE") && !e) return -1;  // a forced launch-per-K tile shape
+  if (e) {
+    if (e[0] == '0') return -1;
+    forced = std::atoi(e) - 1;
+  }
+  for (int v = 0; v < N_PERSIST_CFGS; ++v) {
+    if (forced >= 0 && v != forced) continue;
+    const TileCfg c = PERSIST_CFGS[v];
+    if (forced < 0 && c.k != 8) continue;  // K = 8 by default; K = 4 on request
+    if (nx < c.ti + 2 * c.k || ny < c.tj + 2 * c.k) continue;
+    const int tiles = ((nx + c.ti - 1) / c.ti) * ((ny + c.tj - 1) / c.tj);
+    if (tiles <= persist_capacity<R>(v)) return v;
+  }
+  return -1;
 }
 
 template <typename R>
@@ -867,7 +1078,10 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
     CEV_CHECK_LAUNCH("fdtd run (per step)");
     return CEV_OK;
   }
-  if (!p->shadow) CEV_CUDA(cudaMalloc(&p->shadow, 6 * N * sizeof(R)));
+  if (!p->shadow) {
+    CEV_REQUIRE(!p->borrowed, "borrowed FDTD plan without a shadow state");
+    CEV_CUDA(cudaMalloc(&p->shadow, 6 * N * sizeof(R)));
+  }
   R* sh = (R*)p->shadow;
   R* bufA[6] = {(R*)st->hx, (R*)st->hy, (R*)st->dz, (R*)st->icex, (R*)st->icey, (R*)st->idz};
   R* bufB[6] = {sh, sh + N, sh + 2 * N, sh + 3 * N, sh + 4 * N, sh + 5 * N};
@@ -875,13 +1089,72 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
   CEV_CUDA(cudaMemcpyAsync(bufB[3], bufA[3], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   CEV_CUDA(cudaMemcpyAsync(bufB[4], bufA[4], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   CEV_CUDA(cudaMemcpyAsync(bufB[5], bufA[5], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
-  static bool prepared[2][N_TILE_CFGS] = {};
-  static bool prepared_hist[2] = {};
+  // single launch for grids whose tiles all fit on the GPU at once
+  const int pc = (dz_hist || p->borrowed) ? -1 : pick_persist<R>(p->nx, p->ny);
+  if (pc >= 0 && nsteps > PERSIST_CFGS[pc].k) {
+    const TileCfg c = PERSIST_CFGS[pc];
+    const int gy = (p->nx + c.ti - 1) / c.ti, gx = (p->ny + c.tj - 1) / c.tj;
+    if (p->pcfg != pc) {
+      std::vector<int> nbr;
+      if (persist_neighbours(p->nx, p->ny, c, nbr)) {
+        cudaFree(p->pnbr);
+        cudaFree(p->pflags);
+        p->pnbr = nullptr;
+        p->pflags = nullptr;
+        p->pcfg = -1;
+        CEV_CUDA(cudaMalloc(&p->pnbr, sizeof(int) * nbr.size()));
+        CEV_CUDA(cudaMemcpy(p->pnbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice));
+        CEV_CUDA(cudaMalloc(&p->pflags, sizeof(int) * (gx * gy + 1)));
+        p->pcfg = pc;
+        p->ptiles = gx * gy;
+      }
+    }
+    if (p->pcfg == pc) {
+      TBArgs<R> a{};
+      a.nx = p->nx; a.ny = p->ny; a.K = c.k; a.t0 = 0;
+      a.hx_i = bufA[0]; a.hy_i = bufA[1]; a.dz_i = bufA[2];
+      a.icex_i = bufA[3]; a.icey_i = bufA[4]; a.idz_i = bufA[5];
+      a.iez = (const R*)p->iez;
+      a.ax = (const AxisCoef<R>*)p->ax;
+      a.ay = (const AxisCoef<R>*)p->ay;
+      a.S = (R)p->S;
+      a.ns = ns;
+      a.src_idx = ns ? io->src_idx : nullptr;
+      a.src_w = ns ? (const R*)io->src_w : nullptr;
+      a.amps = ns ? (const R*)io->amps : nullptr;
+      a.np = np;
+      a.probe_idx = np ? io->probe_idx : nullptr;
+      a.probe_out = np ? (R*)io->probe_out : nullptr;
+      a.nsteps = nsteps;
+      for (int f = 0; f < 6; ++f) {
+        a.xb[0][f] = bufB[f];
+        a.xb[1][f] = bufA[f];
+      }
+      a.flags = p->pflags;
+      a.fault = p->pflags + p->ptiles;
+      a.nbr = p->pnbr;
+      CEV_CUDA(cudaMemsetAsync(p->pflags, 0, sizeof(int) * (p->ptiles + 1), s));
+      int rc = persist_launch<R>(pc, dim3(gx, gy, 1), a, s);
+      if (rc != CEV_OK) return rc;
+      const int nblk = (nsteps + c.k - 1) / c.k;
+      if (((nblk - 1) & 1) == 0)  // the last block went to the shadow buffer
+        for (int f = 0; f < 6; ++f)
+          CEV_CUDA(cudaMemcpyAsync(bufA[f], bufB[f], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+      int fault = 0;
+      CEV_CUDA(cudaMemcpyAsync(&fault, a.fault, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CEV_CUDA(cudaStreamSynchronize(s));
+      if (fault) {
+        set_error("persistent FDTD runner: a tile's neighbour wait ran out (exchange fault)");
+        return CEV_ERR_CUDA;
+      }
+      return CEV_OK;
+    }
+  }
   TBArgs<R> a{};
-  if (dz_hist ? !prepared_hist[sizeof(R) == 8] : !prepared[sizeof(R) == 8][cfg]) {
+  {
+    // per device and kernel, thread-safe (allow_dynamic_smem)
     int rc = dz_hist ? hist_launch<R>(true, dim3(), a, s) : tile_dispatch<R>(cfg, true, dim3(), a, s);
     if (rc != CEV_OK) return rc;
-    (dz_hist ? prepared_hist[sizeof(R) == 8] : prepared[sizeof(R) == 8][cfg]) = true;
   }
   const TileCfg tc = TILE_CFGS[cfg];
   const int K = tc.k;
@@ -1056,6 +1329,8 @@ int cev_fdtd_plan_create(cev_fdtd_plan* out, int nx, int ny, double dL, int npml
 
 int cev_fdtd_plan_destroy(cev_fdtd_plan p) {
   if (!p) return CEV_OK;
+  cudaFree(p->pnbr);
+  cudaFree(p->pflags);
   cudaFree(p->ax);
   cudaFree(p->ay);
   cudaFree(p->iez);
@@ -1227,6 +1502,40 @@ __global__ void k_inv_ezz_f32(const double* eps, float* iez, size_t N) {
 }  // namespace
 }  // namespace cev
 
+namespace cev {
+// AxisCoef<float>[N] of one axis computed on the device from (N, npml, dt, S):
+// the sigma loop of ceviche/fdtd.py:224-263 keeps, for every 2X-grid index, the
+// value of its last write (the largest loop index n that writes it), then the
+// coefficients of axis_coefs.  Lets the allocation-free runner build its
+// tables without host-to-device copies.
+__global__ void k_axis_coef_f32(AxisCoef<float>* out, int N, int npml, double dt, double S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  auto s2 = [&](int k) -> double {
+    int n = -1;
+    const int n1 = 2 * npml + 1 - k;       // written as k1 = 2 npml - n + 1
+    const int n2 = k - 2 * N + 2 * npml;   // written as k2 = 2N - 2 npml + n
+    if (n1 >= 0 && n1 < 2 * npml) n = n1;
+    if (n2 >= 0 && n2 < 2 * npml && n2 >= n) n = n2;
+    if (n < 0) return 0.0;
+    const double x = (double)n / 2 / npml;
+    return (0.5 * F_EPSILON_0 / dt) * (x * x * x);
+  };
+  const double h = s2(2 * i + 1) * dt / (2 * F_EPSILON_0);
+  const double d = s2(2 * i) * dt / (2 * F_EPSILON_0);
+  AxisCoef<float> c;
+  c.aH = (float)h;
+  c.f1H = (float)((1 - h) / (1 + h));
+  c.f2H = (float)(S / (1 + h));
+  c.pH = (float)(1 / (1 + h));
+  c.aD = (float)d;
+  c.f1D = (float)((1 - d) / (1 + d));
+  c.f2D = (float)(S / (1 + d));
+  c.pD = (float)(1 / (1 + d));
+  out[i] = c;
+}
+}  // namespace cev
+
 extern "C" CEV_API int cev_fdtd_run_tm_noalloc(int nx, int ny, double dL, int npml_x, int npml_y,
                                                const double* eps, const cev_fdtd_state* st,
                                                int nsteps, const cev_fdtd_io* io,
@@ -1264,16 +1573,13 @@ extern "C" CEV_API int cev_fdtd_run_tm_noalloc(int nx, int ny, double dL, int np
   p.dt = fdtd_dt(dL);
   const double C_0 = 1.0 / std::sqrt(F_EPSILON_0 * F_MU_0);
   p.S = C_0 * p.dt / dL;
-  sigma_profile(nx, npml_x, p.dt, p.aHx, p.aDx);
-  sigma_profile(ny, npml_y, p.dt, p.aHy, p.aDy);
-  const auto cx = axis_coefs<float>(p.aHx, p.aDx, p.S);
-  const auto cy = axis_coefs<float>(p.aHy, p.aDy, p.S);
   const size_t N = (size_t)nx * ny;
   AxisCoef<float>* ax = sp.axis;
   AxisCoef<float>* ay = sp.axis + NOALLOC_MAX_DIM;
-  // pageable-source copies: staged by the driver before the call returns
-  CEV_CUDA(cudaMemcpyAsync(ax, cx.data(), cx.size() * sizeof(cx[0]), cudaMemcpyHostToDevice, s));
-  CEV_CUDA(cudaMemcpyAsync(ay, cy.data(), cy.size() * sizeof(cy[0]), cudaMemcpyHostToDevice, s));
+  // tables built on the device: the call issues no host-to-device copy
+  k_axis_coef_f32<<<ceil_div(nx, 256), 256, 0, s>>>(ax, nx, npml_x, p.dt, p.S);
+  k_axis_coef_f32<<<ceil_div(ny, 256), 256, 0, s>>>(ay, ny, npml_y, p.dt, p.S);
+  CEV_CHECK_LAUNCH("k_axis_coef_f32");
   float* iez = sp.scratch + 6 * NOALLOC_MAX_CELLS;
   k_inv_ezz_f32<<<std::max(1u, std::min(ceil_div(N, 256), 8u * sm_count())), 256, 0, s>>>(eps, iez,
                                                                                           N);
@@ -1281,7 +1587,8 @@ extern "C" CEV_API int cev_fdtd_run_tm_noalloc(int nx, int ny, double dL, int np
   p.ax = ax;
   p.ay = ay;
   p.iez = iez;
-  p.shadow = sp.scratch;  // run_tm_impl uses 6N floats from here and never allocates
+  p.shadow = sp.scratch;  // run_tm_impl uses 6N floats from here
+  p.borrowed = true;      // ... and, for a borrowed plan, never allocates
   rc = run_tm_impl<float>(&p, st, nsteps, io, s);
   p.ax = p.ay = p.iez = p.shadow = nullptr;  // not owned: nothing for the host struct to free
   return rc;

@@ -1049,14 +1049,13 @@ static int g_conv_nonpersistent = 0;  // 1: single-slab layers also use k_conv3_
 template <int BN>
 static int launch_conv_tcp(const ConvArgs& a, cudaStream_t s) {
   constexpr int smem = 9 * TcGeom<BN>::TAP_B + 2 * HX_SLAB_A;
-  static int per_sm = 0;
-  if (!per_sm) {
-    CEV_CUDA(cudaFuncSetAttribute(k_conv3_tcp<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    CEV_CUDA(cudaFuncSetAttribute(k_conv3_tcp<BN>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
-    // resident CTAs per SM: shared memory (227 KB usable, 1 KB reserved per
-    // CTA) and TMEM (2*BN of 512 columns per CTA)
-    per_sm = std::max(1, std::min((227 * 1024) / (smem + 128 + 1024), 512 / (2 * BN)));
+  {
+    const int rc = allow_dynamic_smem((const void*)k_conv3_tcp<BN>, smem, 100);
+    if (rc != CEV_OK) return rc;
   }
+  // resident CTAs per SM: shared memory (227 KB usable, 1 KB reserved per
+  // CTA) and TMEM (2*BN of 512 columns per CTA)
+  const int per_sm = std::max(1, std::min((227 * 1024) / (smem + 128 + 1024), 512 / (2 * BN)));
   const long long tiles = (long long)((a.H + HX_TI - 1) / HX_TI) * ((a.W + HX_TJ - 1) / HX_TJ) *
                           (a.npix / ((long long)a.H * a.W));
   const int ny = (a.cout + BN - 1) / BN;
@@ -1071,10 +1070,9 @@ template <int BN>
 static int launch_conv_tc(const ConvArgs& a, cudaStream_t s) {
   if (a.cinp == CBK && !g_conv_nonpersistent) return launch_conv_tcp<BN>(a, s);
   constexpr int slab = TcGeom<BN>::SLAB;
-  static bool attr = false;
-  if (!attr) {
-    CEV_CUDA(cudaFuncSetAttribute(k_conv3_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * slab));
-    attr = true;
+  {
+    const int rc = allow_dynamic_smem((const void*)k_conv3_tc<BN>, 2 * slab);
+    if (rc != CEV_OK) return rc;
   }
   const int smem = (a.cinp > CBK ? 2 : 1) * slab;
   const long long tiles = (long long)((a.H + HX_TI - 1) / HX_TI) * ((a.W + HX_TJ - 1) / HX_TJ) *

@@ -42,7 +42,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <vector>
 
 #include "fdfd_plan.hpp"
@@ -709,20 +708,6 @@ static int upload(T** dst, const std::vector<T>& v) {
   return CEV_OK;
 }
 
-// Dynamic shared memory above the 48 KB default, once per device and kernel.
-static int allow_smem(const void* fn, int slot, int bytes) {
-  static std::mutex mu;
-  static int done[64][8] = {};
-  int dev = 0;
-  CEV_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64 || slot < 0 || slot >= 8) return CEV_ERR_INVALID;
-  std::lock_guard<std::mutex> lk(mu);
-  if (done[dev][slot] >= bytes) return CEV_OK;
-  CEV_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  done[dev][slot] = bytes;
-  return CEV_OK;
-}
-
 // Builds the tree, offsets, descriptors, maps and work lists; uploads them
 // when `upload_all` (otherwise only the sizes are filled in: no CUDA call).
 static int analyse(cev_nd_precond_s* h, bool upload_all, size_t* n_nodes = nullptr,
@@ -901,9 +886,9 @@ static Args make_args(const cev_nd_precond_s* h, const Op& op) {
 }
 
 template <int FS, int TR, int TC>
-static int launch_small(const Args& a, const Level& L, int B, cudaStream_t s, int slot) {
+static int launch_small(const Args& a, const Level& L, int B, cudaStream_t s) {
   const int bytes = (FS * FS + 2 * FS) * (int)sizeof(float2);
-  int rc = allow_smem((const void*)k_small<FS, TR, TC>, slot, bytes);
+  int rc = allow_dynamic_smem((const void*)k_small<FS, TR, TC>, bytes);
   if (rc != CEV_OK) return rc;
   k_small<FS, TR, TC><<<dim3((unsigned)L.small.size(), B), TR * TC, bytes, s>>>(a, L.d_small);
   CEV_CHECK_LAUNCH("nd k_small");
@@ -929,9 +914,9 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
     }
     if (!L.small.empty()) {
       int rc;
-      if (L.max_f_small <= 32) rc = launch_small<32, 8, 16>(a, L, B, s, 0);
-      else if (L.max_f_small <= 64) rc = launch_small<64, 16, 16>(a, L, B, s, 1);
-      else rc = launch_small<128, 16, 32>(a, L, B, s, 2);
+      if (L.max_f_small <= 32) rc = launch_small<32, 8, 16>(a, L, B, s);
+      else if (L.max_f_small <= 64) rc = launch_small<64, 16, 16>(a, L, B, s);
+      else rc = launch_small<128, 16, 32>(a, L, B, s);
       if (rc != CEV_OK) return rc;
     }
     if (L.large.empty()) continue;
@@ -969,11 +954,11 @@ int nd_apply(cev_nd_precond_s* h, const float2* v, float2* z, const double* sc, 
     }
     if (!L.large.empty()) {
       const int bytes = L.max_f * (int)sizeof(float2);
-      if ((rc = nd::allow_smem((const void*)nd::k_fwd<false>, 3, bytes)) != CEV_OK) return rc;
+      if ((rc = allow_dynamic_smem((const void*)nd::k_fwd<false>, bytes)) != CEV_OK) return rc;
       nd::k_fwd<false><<<dim3((unsigned)L.large.size(), B), 256, bytes, s>>>(a, io, L.d_large);
       if (!L.gemv.empty()) {
         const int gb = L.max_nI * (int)sizeof(float2);
-        if ((rc = nd::allow_smem((const void*)nd::k_fwd_gemv, 4, gb)) != CEV_OK) return rc;
+        if ((rc = allow_dynamic_smem((const void*)nd::k_fwd_gemv, gb)) != CEV_OK) return rc;
         nd::k_fwd_gemv<<<dim3((unsigned)L.gemv.size(), B), 256, gb, s>>>(a, io, L.d_gemv);
       }
     }
@@ -983,7 +968,7 @@ int nd_apply(cev_nd_precond_s* h, const float2* v, float2* z, const double* sc, 
     const nd::Level& L = h->levels[d];
     if (L.bwd.empty()) continue;
     const int bytes = L.max_f * (int)sizeof(float2);
-    if ((rc = nd::allow_smem((const void*)nd::k_bwd, 5, bytes)) != CEV_OK) return rc;
+    if ((rc = allow_dynamic_smem((const void*)nd::k_bwd, bytes)) != CEV_OK) return rc;
     nd::k_bwd<<<dim3((unsigned)L.bwd.size(), B), 256, bytes, s>>>(a, io, L.d_bwd);
     CEV_CHECK_LAUNCH("nd backward");
   }

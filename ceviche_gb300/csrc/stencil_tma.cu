@@ -19,6 +19,7 @@
 //
 // The wait on the mbarrier is bounded; a timeout records a fault in the
 // problem's KState and the block waits (bounded) again before it exits.
+#include <mutex>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -209,10 +210,10 @@ __global__ void __launch_bounds__(TT_THREADS) k_arnoldi_mv_tma(const __grid_cons
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  // a driver entry point is the same for every device: look it up once
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static std::once_flag once;
+  std::call_once(once, [] {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
@@ -221,7 +222,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
       fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
     else
       cudaGetLastError();
-  }
+  });
   return fn;
 }
 

@@ -55,8 +55,12 @@ def _io(nx, ny, steps, rng):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape", [(128, 112), (40, 36)])
+@pytest.mark.parametrize("shape", [(128, 112), (40, 36), (512, 512), (8192, 32), (32, 8192)])
 def test_noalloc_runner_matches_plan_runner(shape):
+    """(512, 512) fills the static scratch to its cell limit; (8192, 32) and
+    (32, 8192) fill the axis tables to their per-dimension limit.  The
+    runner builds its PML tables on the device, the plan runner on the host:
+    agreement to 1e-6 also checks the tables."""
     lib = _lib_loaded()
     nx, ny = shape
     dL, npml = 25e-9, (9, 7)
