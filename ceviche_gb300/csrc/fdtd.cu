@@ -997,9 +997,10 @@ static int persist_launch(int cfg, dim3 g, TBArgs<R>& a, cudaStream_t s) {
   }
 }
 
-// Symmetric neighbour lists of the tile grid: tile T exchanges with the owner
-// of every ring cell of its region, and the owner with T.  Returns false when
-// some tile has more than NBR_MAX neighbours.
+// Symmetric neighbour lists of the tile grid: tile T exchanges with every
+// tile owning a cell of T's region (the tile rows its region rows fall in
+// times the tile columns its region columns fall in), and each of those with
+// T.  Returns false when some tile has more than NBR_MAX neighbours.
 static bool persist_neighbours(int nx, int ny, const TileCfg& c, std::vector<int>& out) {
   const int gy = (nx + c.ti - 1) / c.ti, gx = (ny + c.tj - 1) / c.tj, tiles = gx * gy;
   const int RI = c.ti + 2 * c.k, RJ = c.tj + 2 * c.k;
@@ -1007,14 +1008,22 @@ static bool persist_neighbours(int nx, int ny, const TileCfg& c, std::vector<int
   auto add = [&](int a, int b) {
     if (std::find(nb[a].begin(), nb[a].end(), b) == nb[a].end()) nb[a].push_back(b);
   };
+  auto touched = [](int g0, int len, int n, int t, std::vector<int>& v) {
+    v.clear();
+    for (int r = 0; r < len; ++r) {
+      const int q = (((g0 + r) % n + n) % n) / t;
+      if (std::find(v.begin(), v.end(), q) == v.end()) v.push_back(q);
+    }
+  };
+  std::vector<int> rows, cols;
   for (int ty = 0; ty < gy; ++ty)
     for (int tx = 0; tx < gx; ++tx) {
-      const int t = ty * gx + tx, gi0 = ty * c.ti - c.k, gj0 = tx * c.tj - c.k;
-      for (int r = 0; r < RI; ++r)
-        for (int q = 0; q < RJ; ++q) {
-          if (r >= c.k && r < c.k + c.ti && q >= c.k && q < c.k + c.tj) continue;
-          const int i = ((gi0 + r) % nx + nx) % nx, j = ((gj0 + q) % ny + ny) % ny;
-          const int o = (i / c.ti) * gx + (j / c.tj);
+      const int t = ty * gx + tx;
+      touched(ty * c.ti - c.k, RI, nx, c.ti, rows);
+      touched(tx * c.tj - c.k, RJ, ny, c.tj, cols);
+      for (int r : rows)
+        for (int q : cols) {
+          const int o = r * gx + q;
           if (o == t) continue;
           add(t, o);
           add(o, t);

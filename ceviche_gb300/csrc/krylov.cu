@@ -146,6 +146,41 @@ __global__ void __launch_bounds__(128) k_arnoldi_mv(MvArgs<POL, E> a) {
                              a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
 }
 
+// The exact (FP64) operator on a complex64 input, complex64 output: the
+// matvec of a flexible cycle whose preconditioner is a factorisation.  There
+// z = M^-1 v is larger than A z ~ v by up to cond(A), so a float32 stencil
+// (float tables, float eps, float products) would lose cond(A) * 6e-8 of the
+// Arnoldi relation to cancellation.
+template <int POL, typename E>
+struct Mv64Args {
+  int nx, ny, rows;
+  const E* eps;
+  size_t eps_bs;
+  const float2* in;
+  float2* out;
+  size_t bs;
+  const Coef<double>* cx;
+  const Coef<double>* cy;
+  const double* k2;
+  const KState* st;
+};
+
+template <int POL, typename E>
+__global__ void __launch_bounds__(128) k_arnoldi_mv64(Mv64Args<POL, E> a) {
+  const int b = blockIdx.z;
+  if (!a.st[b].active) return;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.ny) return;
+  const int i0 = blockIdx.y * a.rows;
+  const int i1 = min(i0 + a.rows, a.nx);
+  const float2* x = a.in + b * a.bs;
+  float2* y = a.out + b * a.bs;
+  const Coef<double> cyj = a.cy[(size_t)b * a.ny + j];
+  auto ep = [&](int i, double2 v, double2) { y[(size_t)i * a.ny + j] = to_f(v); };
+  stencil_column<double, POL, decltype(ep), false, E, float2>(
+      a.nx, a.ny, j, i0, i1, x, a.eps + b * a.eps_bs, a.cx + (size_t)b * a.nx, cyj, a.k2[b], ep);
+}
+
 // ----------------------------------------------------------- multi-dot
 // d_k = sum_n conj(V_k[n]) w[n], k = 0..j ; H[j][k] (+)= sc_k d_k
 struct DotArgs {
@@ -802,8 +837,28 @@ int cev_fdfd_solve(cev_fdfd_plan p, const double* eps, int eps_shared, const voi
     return CEV_OK;
   };
   const bool tma_mv = tma_matvec_usable(p, ce);
+  const bool exact_mv =
+      o.precond == CEV_PRECOND_DIRECT || o.precond == CEV_PRECOND_SHIFTED_LAPLACIAN;
   ops.matvec = [&](const KCtx& c, int j, const float2* in, int use_scale, float2* out,
                    cudaStream_t st) -> int {
+    if (exact_mv && !use_scale) {
+      auto go = [&](auto pol_tag, auto e_tag) {
+        constexpr int POL = decltype(pol_tag)::value;
+        using E = decltype(e_tag);
+        Mv64Args<POL, E> a{p->nx, p->ny, rows, (const E*)eps, ebs, in, out, N,
+                           p->cx64[tr], p->cy64[tr], p->k2_64, c.st};
+        k_arnoldi_mv64<POL, E><<<sg, sb, 0, st>>>(a);
+      };
+      if (p->pol == POL_EZ) {
+        if (ce) go(std::integral_constant<int, POL_EZ>{}, double2{});
+        else go(std::integral_constant<int, POL_EZ>{}, double{});
+      } else {
+        if (ce) go(std::integral_constant<int, POL_HZ>{}, double2{});
+        else go(std::integral_constant<int, POL_HZ>{}, double{});
+      }
+      CEV_CHECK_LAUNCH("k_arnoldi_mv64");
+      return CEV_OK;
+    }
     // TMA needs 16-byte aligned operands; anything else takes the column sweep
     if (tma_mv && (((uintptr_t)in | (uintptr_t)eps32) & 15) == 0)
       return tma_matvec(p, tr, eps32, eps_shared, in, out, c, m, j, use_scale, st);

@@ -42,6 +42,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
+#include <mutex>
 #include <vector>
 
 #include "fdfd_plan.hpp"
@@ -51,11 +53,16 @@ namespace cev {
 namespace nd {
 
 constexpr int LEAF = 4;        // boxes with both sides <= LEAF are eliminated whole
-constexpr int NB = 32;         // pivots per block step of the large-front path
+constexpr int NB = 32;         // pivots per block step of the large-front path (one warp)
 constexpr int SMALL_F = 128;   // fronts up to this size are swept in shared memory
 constexpr int TILE = 64;       // update tile (rows x cols) of the large-front path
-constexpr int GEMV_ROWS = 32;  // rows per CTA of the apply GEMVs
+constexpr int GEMV_ROWS = 32;  // rows per CTA of the large-front apply GEMVs
+constexpr int WPB = 8;         // warps (small fronts) per CTA of the apply kernels
 
+// Factor storage of a small front (f <= SMALL_F) is column-major, so its
+// apply runs one warp per front with a lane per row (coalesced, no
+// reductions); a large front is row-major (warp per row, coalesced along the
+// row, and the blocked sweep addresses rows).
 struct Node {
   int nI, nB;
   int cells;         // offset in the cell list: nI interior then nB boundary cells
@@ -63,14 +70,11 @@ struct Node {
   int cmap[2];       // offset in the map list: child's B cells -> positions in this front
   int desc, ndesc;   // original-entry descriptors
   int par;           // Schur arena of this node's depth (depth & 1)
-  int pad;
-  long long top;     // [G | H] (nI x f) of problem 0; problem b adds b * fst
-  long long bl;      // -K (nB x nI) of problem 0
-  long long fst;     // factor stride between problems at this depth
-  long long s;       // S (nB x nB) in arena par, problem 0; problem b adds b * sst
-  long long sst;
-  long long fv;      // front vector (f) of problem 0; problem b adds b * fvst
-  long long fvst;
+  int small;         // f <= SMALL_F
+  long long top;     // [G | H] (nI x f), offset within one problem's factor block
+  long long bl;      // -K (nB x nI)
+  long long s;       // S (nB x nB, row-major) within one problem's block of arena par
+  long long fv;      // front vector (f) within one problem's block
 };
 
 // A'(row cell, neighbour in direction dir) of one stencil row:
@@ -102,6 +106,7 @@ struct Args {
   float2* fv;
   int* fault;  // set when a pivot is zero or not finite
   size_t n;    // cells per problem
+  long long fac_pp, sa_pp[2], fv_pp;  // per-problem strides
 };
 
 __device__ __forceinline__ float2 eps_at(const Op& o, int b, int i, int j) {
@@ -168,24 +173,47 @@ __device__ __forceinline__ void check_pivot(const Args& a, float2 d) {
   if (!(m > 0.f) || !isfinite(m)) atomicExch(a.fault, 1);
 }
 
-// Address of front entry (r, c) of node n for problem b (large-front path).
+__device__ __forceinline__ float2* ftop(const Args& a, const Node& n, int b) {
+  return a.fac + (long long)b * a.fac_pp + n.top;
+}
+__device__ __forceinline__ float2* fbl(const Args& a, const Node& n, int b) {
+  return a.fac + (long long)b * a.fac_pp + n.bl;
+}
+__device__ __forceinline__ float2* fsch(const Args& a, const Node& n, int b) {
+  return a.sar[n.par] + (long long)b * a.sa_pp[n.par] + n.s;
+}
+__device__ __forceinline__ float2* ffv(const Args& a, const Node& n, int b) {
+  return a.fv + (long long)b * a.fv_pp + n.fv;
+}
+
+// Address of front entry (r, c) of a large node n for problem b.
 __device__ __forceinline__ float2* fel(const Args& a, const Node& n, int b, int r, int c) {
   const int f = n.nI + n.nB;
-  if (r < n.nI) return a.fac + n.top + (long long)b * n.fst + (long long)r * f + c;
+  if (r < n.nI) return ftop(a, n, b) + (long long)r * f + c;
   r -= n.nI;
-  if (c < n.nI) return a.fac + n.bl + (long long)b * n.fst + (long long)r * n.nI + c;
-  return a.sar[n.par] + n.s + (long long)b * n.sst + (long long)r * n.nB + (c - n.nI);
+  if (c < n.nI) return fbl(a, n, b) + (long long)r * n.nI + c;
+  return fsch(a, n, b) + (long long)r * n.nB + (c - n.nI);
+}
+
+// Zero [lo, lo + len) of every problem's block (stride pp elements).
+__global__ void k_zero(float2* base, long long pp, long long lo, long long len, int B) {
+  const long long total = len * B;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long b = e / len, k = e - b * len;
+    base[b * pp + lo + k] = make_float2(0.f, 0.f);
+  }
 }
 
 // ============================================================ small fronts
 // One CTA per (node, problem): assemble F (f <= FS) in shared memory, keep
 // each thread's TR x TC-strided block of it in registers through the
-// Gauss-Jordan sweep, write [G | H], -K and S out.
+// Gauss-Jordan sweep, write [G | H] and -K (column-major) and S out.
 template <int FS, int TR, int TC>
 __global__ void __launch_bounds__(TR * TC) k_small(Args a, const int* __restrict__ list) {
   constexpr int R = FS / TR, Cn = FS / TC;
   extern __shared__ float2 sm[];
-  float2* F = sm;                // f x f, row stride f
+  float2* F = sm;                 // f x f, row stride f
   float2* rowbuf = sm + FS * FS;  // FS
   float2* colbuf = rowbuf + FS;   // FS
   __shared__ float2 s_pinv;
@@ -202,11 +230,13 @@ __global__ void __launch_bounds__(TR * TC) k_small(Args a, const int* __restrict
     t = cadd(t, v);
   }
   __syncthreads();
+#pragma unroll
   for (int s = 0; s < 2; ++s) {
-    if (n.child[s] < 0) continue;
-    const Node c = a.nodes[n.child[s]];
+    const int ch = n.child[s];
+    if (ch < 0) continue;
+    const Node c = a.nodes[ch];
     const int* map = a.cmap + n.cmap[s];
-    const float2* S = a.sar[c.par] + c.s + (long long)b * c.sst;
+    const float2* S = fsch(a, c, b);
     for (int e = tid; e < c.nB * c.nB; e += nt) {
       const int r = e / c.nB, q = e - r * c.nB;
       float2& t = F[map[r] * f + map[q]];
@@ -268,17 +298,17 @@ __global__ void __launch_bounds__(TR * TC) k_small(Args a, const int* __restrict
       }
     }
   }
-  float2* top = a.fac + n.top + (long long)b * n.fst;
-  float2* bl = a.fac + n.bl + (long long)b * n.fst;
-  float2* S = a.sar[n.par] + n.s + (long long)b * n.sst;
+  float2* top = ftop(a, n, b);
+  float2* bl = fbl(a, n, b);
+  float2* S = fsch(a, n, b);
 #pragma unroll
   for (int u = 0; u < R; ++u)
 #pragma unroll
     for (int v = 0; v < Cn; ++v) {
       const int r = ty + TR * u, c = tx + TC * v;
       if (r >= f || c >= f) continue;
-      if (r < nI) top[(size_t)r * f + c] = reg[u][v];
-      else if (c < nI) bl[(size_t)(r - nI) * nI + c] = reg[u][v];
+      if (r < nI) top[(size_t)c * nI + r] = reg[u][v];                  // column-major [G | H]
+      else if (c < nI) bl[(size_t)c * nB + (r - nI)] = reg[u][v];       // column-major -K
       else S[(size_t)(r - nI) * nB + (c - nI)] = reg[u][v];
     }
 }
@@ -301,10 +331,12 @@ __global__ void k_extend(Args a, const int2* __restrict__ work, int slot) {
   const int2 w = work[blockIdx.x];
   const Node n = a.nodes[w.x];
   const int b = blockIdx.y;
-  const Node c = a.nodes[n.child[slot]];
-  const int* map = a.cmap + n.cmap[slot];
+  const int ch = slot == 0 ? n.child[0] : n.child[1];
+  const int cm = slot == 0 ? n.cmap[0] : n.cmap[1];
+  const Node c = a.nodes[ch];
+  const int* map = a.cmap + cm;
   const int r = w.y;
-  const float2* S = a.sar[c.par] + c.s + (long long)b * c.sst + (long long)r * c.nB;
+  const float2* S = fsch(a, c, b) + (long long)r * c.nB;
   const int pr = map[r];
   for (int q = threadIdx.x; q < c.nB; q += blockDim.x) {
     float2* t = fel(a, n, b, pr, map[q]);
@@ -312,51 +344,51 @@ __global__ void k_extend(Args a, const int2* __restrict__ work, int slot) {
   }
 }
 
-// In-place inverse of the pivot block F[k0:k0+nb, k0:k0+nb] (Gauss-Jordan).
-__global__ void __launch_bounds__(256) k_pivblock(Args a, const int* __restrict__ list, int k0) {
-  __shared__ float2 blk[NB][NB + 1];
-  __shared__ float2 rowb[NB], colb[NB];
-  __shared__ float2 s_pinv;
-  const Node n = a.nodes[list[blockIdx.x]];
+__device__ __forceinline__ float2 shfl2(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// In-place inverse of the pivot block F[k0:k0+nb, k0:k0+nb], one warp per
+// (node, problem): lane j holds column j in registers (padded with the
+// identity to 32 x 32), Gauss-Jordan with the pivot column broadcast by shuffles.
+__global__ void __launch_bounds__(128) k_pivblock(Args a, const int* __restrict__ list, int count,
+                                                  int k0) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * 4 + warp;
+  if (item >= count) return;
+  const Node n = a.nodes[list[item]];
   if (k0 >= n.nI) return;
   const int b = blockIdx.y;
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
-  float2* base = a.fac + n.top + (long long)b * n.fst;
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int r = e / nb, c = e - r * nb;
-    blk[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
-  }
-  __syncthreads();
-  for (int p = 0; p < nb; ++p) {
-    if (threadIdx.x == 0) {
-      check_pivot(a, blk[p][p]);
-      s_pinv = crcp(blk[p][p]);
-    }
-    __syncthreads();
-    const float2 pinv = s_pinv;
-    if (threadIdx.x < nb) {
-      rowb[threadIdx.x] = cmul(blk[p][threadIdx.x], pinv);
-      colb[threadIdx.x] = blk[threadIdx.x][p];
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-      const int r = e / nb, c = e - r * nb;
-      if (r == p) {
-        blk[r][c] = (c == p) ? pinv : rowb[c];
-      } else if (c == p) {
-        const float2 t = cmul(colb[r], pinv);
-        blk[r][c] = make_float2(-t.x, -t.y);
+  float2* base = ftop(a, n, b);
+  float2 reg[NB];
+#pragma unroll
+  for (int r = 0; r < NB; ++r)
+    reg[r] = (r < nb && lane < nb) ? base[(size_t)(k0 + r) * f + k0 + lane]
+                                   : make_float2(r == lane ? 1.f : 0.f, 0.f);
+#pragma unroll
+  for (int p = 0; p < NB; ++p) {
+    const float2 d = shfl2(reg[p], p);
+    if (p < nb && lane == 0) check_pivot(a, d);
+    const float2 pinv = crcp(d);
+    const float2 rp = cmul(reg[p], pinv);  // this lane's entry of the scaled pivot row
+#pragma unroll
+    for (int r = 0; r < NB; ++r) {
+      if (r == p) continue;
+      const float2 c = shfl2(reg[r], p);  // pivot column entry of row r
+      if (lane == p) {
+        const float2 t = cmul(c, pinv);
+        reg[r] = make_float2(-t.x, -t.y);
       } else {
-        const float2 t = cmul(colb[r], rowb[c]);
-        blk[r][c] = csub(blk[r][c], t);
+        reg[r] = csub(reg[r], cmul(c, rp));
       }
     }
-    __syncthreads();
+    reg[p] = (lane == p) ? pinv : rp;
   }
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int r = e / nb, c = e - r * nb;
-    base[(size_t)(k0 + r) * f + k0 + c] = blk[r][c];
-  }
+  if (lane < nb)
+#pragma unroll
+    for (int r = 0; r < NB; ++r)
+      if (r < nb) base[(size_t)(k0 + r) * f + k0 + lane] = reg[r];
 }
 
 // Pivot rows: F[p, c] = Ainv F[p, c] for the 64 columns of one chunk outside
@@ -370,7 +402,7 @@ __global__ void __launch_bounds__(256) k_rowpanel(Args a, const int2* __restrict
   const int b = blockIdx.y;
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
   const int c0 = w.y * TILE;
-  float2* base = a.fac + n.top + (long long)b * n.fst;
+  float2* base = ftop(a, n, b);
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int r = e / nb, c = e - r * nb;
     Ai[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
@@ -410,7 +442,7 @@ __global__ void __launch_bounds__(128) k_update(Args a, const int2* __restrict__
     const int r = r0 + i;
     Cp[i][k] = (r < f && k < nb) ? *fel(a, n, b, r, k0 + k) : make_float2(0.f, 0.f);
   }
-  const float2* rows = a.fac + n.top + (long long)b * n.fst;
+  const float2* rows = ftop(a, n, b);
   for (int e = threadIdx.x; e < NB * TILE; e += blockDim.x) {
     const int k = e / TILE, j = e - k * TILE;
     const int c = c0 + j;
@@ -465,7 +497,7 @@ __global__ void __launch_bounds__(256) k_colpanel(Args a, const int2* __restrict
   const int b = blockIdx.y;
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
   const int r0 = w.y * TILE;
-  const float2* base = a.fac + n.top + (long long)b * n.fst;
+  const float2* base = ftop(a, n, b);
   for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
     const int r = e / nb, c = e - r * nb;
     Ai[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
@@ -499,48 +531,116 @@ __device__ __forceinline__ bool skip(const ApplyIO& io, int b) {
   return io.st != nullptr && !io.st[b].active;
 }
 
-// Forward gather: f = [s v_I ; 0] + children's update vectors, written to the
-// node's front vector; with GEMV, also u = f_B + (-K) f_I (small fronts).
-template <bool GEMV>
-__global__ void __launch_bounds__(256) k_fwd(Args a, ApplyIO io, const int* __restrict__ list) {
+__device__ __forceinline__ float in_scale(const ApplyIO& io, int b) {
+  return io.sc ? (float)io.sc[(size_t)b * io.sc_stride + io.sc_index] : 1.f;
+}
+
+// Front vector f = [s v_I ; 0] + the children's update vectors, in fvs
+// (lanes or threads stride by `step`); callers sync before reading it.
+__device__ __forceinline__ void gather_front(const Args& a, const ApplyIO& io, const Node& n, int b,
+                                             float2* fvs, int t0, int step, bool warp_only) {
+  const int f = n.nI + n.nB;
+  const float s = in_scale(io, b);
+  const int* cl = a.cells + n.cells;
+  const float2* v = io.v + (size_t)b * a.n;
+  for (int t = t0; t < f; t += step) fvs[t] = t < n.nI ? cscale(v[cl[t]], s) : make_float2(0.f, 0.f);
+  if (warp_only) __syncwarp(); else __syncthreads();
+#pragma unroll
+  for (int sl = 0; sl < 2; ++sl) {
+    const int ch = n.child[sl];
+    if (ch < 0) continue;
+    const Node c = a.nodes[ch];
+    const int* map = a.cmap + n.cmap[sl];
+    const float2* u = ffv(a, c, b) + c.nI;
+    for (int t = t0; t < c.nB; t += step) {
+      float2& d = fvs[map[t]];
+      d = cadd(d, u[t]);
+    }
+    if (warp_only) __syncwarp(); else __syncthreads();
+  }
+}
+
+// Forward, small fronts: one warp per (front, problem); lane r computes
+// u[r] = f_B[r] + sum_k (-K)[r][k] f_I[k] from the column-major -K.
+__global__ void __launch_bounds__(WPB * 32) k_fwd_small(Args a, ApplyIO io,
+                                                        const int* __restrict__ list, int count) {
+  __shared__ float2 buf[WPB][SMALL_F];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * WPB + warp;
+  const int b = blockIdx.y;
+  if (item >= count || skip(io, b)) return;
+  const Node n = a.nodes[list[item]];
+  float2* fvs = buf[warp];
+  gather_front(a, io, n, b, fvs, lane, 32, true);
+  const float2* K = fbl(a, n, b);
+  float2* out = ffv(a, n, b);
+  for (int r = lane; r < n.nB; r += 32) {
+    float2 acc = fvs[n.nI + r];
+    for (int k = 0; k < n.nI; ++k) acc = cfma(K[(size_t)k * n.nB + r], fvs[k], acc);
+    out[n.nI + r] = acc;
+  }
+  for (int t = lane; t < n.nI; t += 32) out[t] = fvs[t];
+}
+
+// Backward, small fronts: one warp per (front, problem); lane r computes
+// x_I[r] = sum_k [G | H][r][k] w[k], w = [f_I ; -x_B], from the column-major factor.
+__global__ void __launch_bounds__(WPB * 32) k_bwd_small(Args a, ApplyIO io,
+                                                        const int* __restrict__ list, int count) {
+  __shared__ float2 buf[WPB][SMALL_F];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * WPB + warp;
+  const int b = blockIdx.y;
+  if (item >= count || skip(io, b)) return;
+  const Node n = a.nodes[list[item]];
+  const int f = n.nI + n.nB;
+  float2* wv = buf[warp];
+  const float2* fvn = ffv(a, n, b);
+  const int* cl = a.cells + n.cells;
+  float2* z = io.z + (size_t)b * a.n;
+  for (int t = lane; t < f; t += 32) {
+    if (t < n.nI) {
+      wv[t] = fvn[t];
+    } else {
+      const float2 x = z[cl[t]];
+      wv[t] = make_float2(-x.x, -x.y);
+    }
+  }
+  __syncwarp();
+  const float2* T = ftop(a, n, b);
+  for (int r = lane; r < n.nI; r += 32) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int k = 0; k < f; ++k) acc = cfma(T[(size_t)k * n.nI + r], wv[k], acc);
+    z[cl[r]] = acc;
+  }
+}
+
+// Forward gather of a large front (one CTA per front and problem).
+__global__ void __launch_bounds__(256) k_fwd_large(Args a, ApplyIO io, const int* __restrict__ list) {
   extern __shared__ float2 fvs[];
   const Node n = a.nodes[list[blockIdx.x]];
   const int b = blockIdx.y;
   if (skip(io, b)) return;
-  const int f = n.nI + n.nB;
-  const float s = io.sc ? (float)io.sc[(size_t)b * io.sc_stride + io.sc_index] : 1.f;
-  const int* cl = a.cells + n.cells;
-  const float2* v = io.v + (size_t)b * a.n;
-  for (int t = threadIdx.x; t < f; t += blockDim.x)
-    fvs[t] = t < n.nI ? cscale(v[cl[t]], s) : make_float2(0.f, 0.f);
-  __syncthreads();
-  for (int sl = 0; sl < 2; ++sl) {
-    if (n.child[sl] < 0) continue;
-    const Node c = a.nodes[n.child[sl]];
-    const int* map = a.cmap + n.cmap[sl];
-    const float2* u = a.fv + c.fv + (long long)b * c.fvst + c.nI;
-    for (int t = threadIdx.x; t < c.nB; t += blockDim.x) {
-      float2& d = fvs[map[t]];
-      d = cadd(d, u[t]);
-    }
-    __syncthreads();
+  gather_front(a, io, n, b, fvs, threadIdx.x, blockDim.x, false);
+  float2* out = ffv(a, n, b);
+  for (int t = threadIdx.x; t < n.nI + n.nB; t += blockDim.x) out[t] = fvs[t];
+}
+
+// Row dot product of a warp: sum_k row[k] x[k], four independent partial sums.
+__device__ __forceinline__ float2 warp_dot(const float2* __restrict__ row, const float2* x, int len,
+                                           int lane) {
+  float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
+  int k = lane;
+  for (; k + 96 < len; k += 128) {
+    a0 = cfma(row[k], x[k], a0);
+    a1 = cfma(row[k + 32], x[k + 32], a1);
+    a2 = cfma(row[k + 64], x[k + 64], a2);
+    a3 = cfma(row[k + 96], x[k + 96], a3);
   }
-  float2* out = a.fv + n.fv + (long long)b * n.fvst;
-  if (GEMV) {
-    const float2* K = a.fac + n.bl + (long long)b * n.fst;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int r = warp; r < n.nB; r += nw) {
-      float2 acc = make_float2(0.f, 0.f);
-      const float2* row = K + (size_t)r * n.nI;
-      for (int k = lane; k < n.nI; k += 32) acc = cfma(row[k], fvs[k], acc);
-      acc.x = warp_sumf(acc.x);
-      acc.y = warp_sumf(acc.y);
-      if (lane == 0) out[n.nI + r] = cadd(fvs[n.nI + r], acc);
-    }
-    for (int t = threadIdx.x; t < n.nI; t += blockDim.x) out[t] = fvs[t];
-  } else {
-    for (int t = threadIdx.x; t < f; t += blockDim.x) out[t] = fvs[t];
-  }
+  for (; k < len; k += 32) a0 = cfma(row[k], x[k], a0);
+  float2 acc = cadd(cadd(a0, a1), cadd(a2, a3));
+  acc.x = warp_sumf(acc.x);
+  acc.y = warp_sumf(acc.y);
+  return acc;
 }
 
 // Forward GEMV of a large front: u[r] += (-K)[r] f_I for GEMV_ROWS rows
@@ -551,31 +651,28 @@ __global__ void __launch_bounds__(256) k_fwd_gemv(Args a, ApplyIO io, const int2
   const Node n = a.nodes[w.x];
   const int b = blockIdx.y;
   if (skip(io, b)) return;
-  float2* fvn = a.fv + n.fv + (long long)b * n.fvst;
+  float2* fvn = ffv(a, n, b);
   for (int t = threadIdx.x; t < n.nI; t += blockDim.x) fi[t] = fvn[t];
   __syncthreads();
-  const float2* K = a.fac + n.bl + (long long)b * n.fst;
+  const float2* K = fbl(a, n, b);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int r1 = min(n.nB, (w.y + 1) * GEMV_ROWS);
   for (int r = w.y * GEMV_ROWS + warp; r < r1; r += nw) {
-    float2 acc = make_float2(0.f, 0.f);
-    const float2* row = K + (size_t)r * n.nI;
-    for (int k = lane; k < n.nI; k += 32) acc = cfma(row[k], fi[k], acc);
-    acc.x = warp_sumf(acc.x);
-    acc.y = warp_sumf(acc.y);
+    const float2 acc = warp_dot(K + (size_t)r * n.nI, fi, n.nI, lane);
     if (lane == 0) fvn[n.nI + r] = cadd(fvn[n.nI + r], acc);
   }
 }
 
-// Backward: x_I = [G | H] [f_I ; -x_B] for GEMV_ROWS rows (work: node, row chunk).
-__global__ void __launch_bounds__(256) k_bwd(Args a, ApplyIO io, const int2* __restrict__ work) {
+// Backward of a large front: x_I = [G | H] [f_I ; -x_B] for GEMV_ROWS rows
+// (work: node, row chunk).
+__global__ void __launch_bounds__(256) k_bwd_large(Args a, ApplyIO io, const int2* __restrict__ work) {
   extern __shared__ float2 wv[];
   const int2 w = work[blockIdx.x];
   const Node n = a.nodes[w.x];
   const int b = blockIdx.y;
   if (skip(io, b)) return;
   const int f = n.nI + n.nB;
-  const float2* fvn = a.fv + n.fv + (long long)b * n.fvst;
+  const float2* fvn = ffv(a, n, b);
   const int* cl = a.cells + n.cells;
   float2* z = io.z + (size_t)b * a.n;
   for (int t = threadIdx.x; t < f; t += blockDim.x) {
@@ -587,117 +684,97 @@ __global__ void __launch_bounds__(256) k_bwd(Args a, ApplyIO io, const int2* __r
     }
   }
   __syncthreads();
-  const float2* T = a.fac + n.top + (long long)b * n.fst;
+  const float2* T = ftop(a, n, b);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int r1 = min(n.nI, (w.y + 1) * GEMV_ROWS);
   for (int r = w.y * GEMV_ROWS + warp; r < r1; r += nw) {
-    float2 acc = make_float2(0.f, 0.f);
-    const float2* row = T + (size_t)r * f;
-    for (int k = lane; k < f; k += 32) acc = cfma(row[k], wv[k], acc);
-    acc.x = warp_sumf(acc.x);
-    acc.y = warp_sumf(acc.y);
+    const float2 acc = warp_dot(T + (size_t)r * f, wv, f, lane);
     if (lane == 0) z[cl[r]] = acc;
   }
 }
 
 // ============================================================ host side
 struct HNode {
-  int x0, x1, y0, y1, depth, parent;
+  int x0, x1, y0, y1, depth;
   int child[2] = {-1, -1};
   std::vector<int> I, B;
 };
 
+static void build_tree(std::vector<HNode>& nodes, int nx, int ny, int x0, int x1, int y0, int y1,
+                       int depth) {
+  // explicit stack: (box, depth, parent, child slot)
+  struct Item {
+    int x0, x1, y0, y1, depth, parent, slot;
+  };
+  std::vector<Item> stack{{x0, x1, y0, y1, depth, -1, 0}};
+  while (!stack.empty()) {
+    const Item it = stack.back();
+    stack.pop_back();
+    if (it.x1 <= it.x0 || it.y1 <= it.y0) continue;
+    const int id = (int)nodes.size();
+    nodes.push_back(HNode());
+    HNode& h = nodes.back();
+    h.x0 = it.x0; h.x1 = it.x1; h.y0 = it.y0; h.y1 = it.y1; h.depth = it.depth;
+    if (it.parent >= 0) {
+      HNode& p = nodes[it.parent];
+      if (p.child[0] < 0) p.child[0] = id; else p.child[1] = id;
+    }
+    const int w = it.x1 - it.x0, hh = it.y1 - it.y0;
+    HNode& g = nodes[id];
+    if (w <= LEAF && hh <= LEAF) {
+      for (int i = it.x0; i < it.x1; ++i)
+        for (int j = it.y0; j < it.y1; ++j) g.I.push_back(i * ny + j);
+    } else if (w >= hh) {
+      const int xs = it.x0 + w / 2;
+      for (int j = it.y0; j < it.y1; ++j) g.I.push_back(xs * ny + j);
+      stack.push_back({xs + 1, it.x1, it.y0, it.y1, it.depth + 1, id, 1});
+      stack.push_back({it.x0, xs, it.y0, it.y1, it.depth + 1, id, 0});
+    } else {
+      const int ys = it.y0 + hh / 2;
+      for (int i = it.x0; i < it.x1; ++i) g.I.push_back(i * ny + ys);
+      stack.push_back({it.x0, it.x1, ys + 1, it.y1, it.depth + 1, id, 1});
+      stack.push_back({it.x0, it.x1, it.y0, ys, it.depth + 1, id, 0});
+    }
+    if (it.x0 > 0) for (int j = it.y0; j < it.y1; ++j) g.B.push_back((it.x0 - 1) * ny + j);
+    if (it.x1 < nx) for (int j = it.y0; j < it.y1; ++j) g.B.push_back(it.x1 * ny + j);
+    if (it.y0 > 0) for (int i = it.x0; i < it.x1; ++i) g.B.push_back(i * ny + it.y0 - 1);
+    if (it.y1 < ny) for (int i = it.x0; i < it.x1; ++i) g.B.push_back(i * ny + it.y1);
+  }
+}
+
 struct Level {
   std::vector<int> small, large;            // node ids
   std::vector<int2> ext[2], panel, tiles;   // large-front work lists
-  std::vector<int2> gemv, bwd;              // apply work lists
-  int max_f_small = 0, max_f = 0, max_nI_large = 0, max_nI = 0;
-  long long fac_stride = 0, s_stride = 0, fv_stride = 0;
-  // device copies
+  std::vector<int2> gemv, bwd;              // large-front apply work lists
+  int max_f_small = 0, max_f_large = 0, max_nI_large = 0;
+  long long fac_lo = 0, fac_len = 0, s_len = 0;  // per-problem ranges of this depth
   int *d_small = nullptr, *d_large = nullptr;
   int2 *d_ext[2] = {nullptr, nullptr}, *d_panel = nullptr, *d_tiles = nullptr;
   int2 *d_gemv = nullptr, *d_bwd = nullptr;
 };
 
-class Tree {
- public:
-  int nx, ny;
-  std::vector<HNode> nodes;
-  int build(int x0, int x1, int y0, int y1, int depth, int parent) {
-    if (x1 <= x0 || y1 <= y0) return -1;
-    const int id = (int)nodes.size();
-    nodes.push_back(HNode());
-    {
-      HNode& h = nodes.back();
-      h.x0 = x0; h.x1 = x1; h.y0 = y0; h.y1 = y1; h.depth = depth; h.parent = parent;
-    }
-    const int w = x1 - x0, hh = y1 - y0;
-    std::vector<int> I;
-    int c0 = -1, c1 = -1;
-    if (w <= LEAF && hh <= LEAF) {
-      for (int i = x0; i < x1; ++i)
-        for (int j = y0; j < y1; ++j) I.push_back(i * ny + j);
-    } else if (w >= hh) {
-      const int xs = x0 + w / 2;
-      for (int j = y0; j < y1; ++j) I.push_back(xs * ny + j);
-      c0 = build(x0, xs, y0, y1, depth + 1, id);
-      c1 = build(xs + 1, x1, y0, y1, depth + 1, id);
-    } else {
-      const int ys = y0 + hh / 2;
-      for (int i = x0; i < x1; ++i) I.push_back(i * ny + ys);
-      c0 = build(x0, x1, y0, ys, depth + 1, id);
-      c1 = build(x0, x1, ys + 1, y1, depth + 1, id);
-    }
-    std::vector<int> B;
-    if (x0 > 0) for (int j = y0; j < y1; ++j) B.push_back((x0 - 1) * ny + j);
-    if (x1 < nx) for (int j = y0; j < y1; ++j) B.push_back(x1 * ny + j);
-    if (y0 > 0) for (int i = x0; i < x1; ++i) B.push_back(i * ny + y0 - 1);
-    if (y1 < ny) for (int i = x0; i < x1; ++i) B.push_back(i * ny + y1);
-    HNode& h = nodes[id];
-    h.I = std::move(I);
-    h.B = std::move(B);
-    int k = 0;
-    if (c0 >= 0) h.child[k++] = c0;
-    if (c1 >= 0) h.child[k++] = c1;
-    return id;
-  }
-};
-
-}  // namespace nd
-}  // namespace cev
-
-using namespace cev;
-using namespace cev::nd;
-
-struct cev_nd_precond_s {
-  int nx = 0, ny = 0, batch = 0, pol = 0, transpose = 0, device = 0;
-  double shift = 0;
-  size_t n = 0;
-  int ndepth = 0;
+// Symbolic part of the factorisation: depends on the grid only, shared by
+// every handle of that grid on a device.
+struct Shape {
+  int nx = 0, ny = 0, device = -1, ndepth = 0;
   std::vector<Level> levels;
   Node* d_nodes = nullptr;
   int* d_cells = nullptr;
   int* d_cmap = nullptr;
   Desc* d_desc = nullptr;
-  float2* fac = nullptr;
-  float2* sar[2] = {nullptr, nullptr};
-  float2* fv = nullptr;
-  int* fault = nullptr;
-  size_t fac_elems = 0, sar_elems[2] = {0, 0}, fv_elems = 0;
-  double flops = 0;  // complex multiply-adds of the factorisation, all problems
-  const cev_fdfd_plan_s* plan = nullptr;
-  ~cev_nd_precond_s() {
+  long long fac_pp = 0, sa_pp[2] = {0, 0}, fv_pp = 0;
+  double cmacs_pp = 0;  // Gauss-Jordan complex multiply-adds per problem
+  size_t n_nodes = 0, n_desc = 0;
+  long long cover[2] = {0, 0};
+  ~Shape() {
+    if (device < 0) return;  // host-only analysis: nothing on a device
     for (auto& L : levels) {
       cudaFree(L.d_small); cudaFree(L.d_large); cudaFree(L.d_ext[0]); cudaFree(L.d_ext[1]);
       cudaFree(L.d_panel); cudaFree(L.d_tiles); cudaFree(L.d_gemv); cudaFree(L.d_bwd);
     }
     cudaFree(d_nodes); cudaFree(d_cells); cudaFree(d_cmap); cudaFree(d_desc);
-    cudaFree(fac); cudaFree(sar[0]); cudaFree(sar[1]); cudaFree(fv); cudaFree(fault);
   }
 };
-
-namespace cev {
-namespace nd {
 
 template <typename T>
 static int upload(T** dst, const std::vector<T>& v) {
@@ -708,71 +785,63 @@ static int upload(T** dst, const std::vector<T>& v) {
   return CEV_OK;
 }
 
-// Builds the tree, offsets, descriptors, maps and work lists; uploads them
-// when `upload_all` (otherwise only the sizes are filled in: no CUDA call).
-static int analyse(cev_nd_precond_s* h, bool upload_all, size_t* n_nodes = nullptr,
-                   size_t* n_desc = nullptr, long long* cover = nullptr) {
-  Tree t;
-  t.nx = h->nx;
-  t.ny = h->ny;
-  t.nodes.reserve(2 * (size_t)h->nx * h->ny / (LEAF * LEAF) + 16);
-  t.build(0, h->nx, 0, h->ny, 0, -1);
-  const int nn = (int)t.nodes.size();
+// Builds the tree, offsets, descriptors, maps and work lists of an nx x ny
+// grid; uploads them when `to_device` (otherwise no CUDA call is made).
+static int analyse(Shape& h, int nx, int ny, bool to_device) {
+  h.nx = nx;
+  h.ny = ny;
+  std::vector<HNode> t;
+  t.reserve(2 * (size_t)nx * ny / (LEAF * LEAF) + 16);
+  build_tree(t, nx, ny, 0, nx, 0, ny, 0);
+  const int nn = (int)t.size();
   int maxd = 0;
-  for (auto& x : t.nodes) maxd = std::max(maxd, x.depth);
-  h->ndepth = maxd + 1;
-  h->levels.assign(h->ndepth, Level());
+  for (auto& x : t) maxd = std::max(maxd, x.depth);
+  h.ndepth = maxd + 1;
+  h.levels.assign(h.ndepth, Level());
+  std::vector<std::vector<int>> by_depth(h.ndepth);
+  for (int k = 0; k < nn; ++k) by_depth[t[k].depth].push_back(k);
   std::vector<Node> dn(nn);
-  std::vector<int> cells, cmap;
-  std::vector<Desc> desc;
-  std::vector<int> pos((size_t)h->nx * h->ny, -1);
-  // per-depth offsets
-  std::vector<long long> fac_off(h->ndepth, 0), s_off(h->ndepth, 0), fv_off(h->ndepth, 0);
-  std::vector<std::vector<int>> by_depth(h->ndepth);
-  for (int k = 0; k < nn; ++k) by_depth[t.nodes[k].depth].push_back(k);
-  const long long B = h->batch;
-  long long fac_base = 0, fv_base = 0;
-  const int nx = h->nx, ny = h->ny;
-  double flops = 0;
-  for (int d = 0; d < h->ndepth; ++d) {
-    Level& L = h->levels[d];
-    long long fo = 0, so = 0, vo = 0;
+  long long fo = 0, vo = 0;
+  double cm = 0;
+  for (int d = 0; d < h.ndepth; ++d) {
+    Level& L = h.levels[d];
+    L.fac_lo = fo;
+    long long so = 0;
     for (int k : by_depth[d]) {
-      const HNode& x = t.nodes[k];
+      const HNode& x = t[k];
       Node& n = dn[k];
       n.nI = (int)x.I.size();
       n.nB = (int)x.B.size();
       const long long f = n.nI + n.nB;
-      n.top = fac_base + fo;
-      n.bl = n.top + (long long)n.nI * f;
+      n.small = f <= SMALL_F ? 1 : 0;
+      n.top = fo;
+      n.bl = fo + (long long)n.nI * f;
       fo += (long long)n.nI * f + (long long)n.nB * n.nI;
       n.par = d & 1;
       n.s = so;
       so += (long long)n.nB * n.nB;
-      n.fv = fv_base + vo;
+      n.fv = vo;
       vo += f;
-      flops += (double)n.nI * f * f;
+      cm += (double)n.nI * f * f;
     }
-    L.fac_stride = fo;
-    L.s_stride = so;
-    L.fv_stride = vo;
-    for (int k : by_depth[d]) {
-      dn[k].fst = fo;
-      dn[k].sst = so;
-      dn[k].fvst = vo;
-    }
-    fac_base += fo * B;
-    fv_base += vo * B;
-    h->sar_elems[d & 1] = std::max(h->sar_elems[d & 1], (size_t)(so * B));
+    L.fac_len = fo - L.fac_lo;
+    L.s_len = so;
+    h.sa_pp[d & 1] = std::max(h.sa_pp[d & 1], so);
   }
-  h->fac_elems = (size_t)fac_base;
-  h->fv_elems = (size_t)fv_base;
-  h->flops = flops * (double)B;
+  h.fac_pp = fo;
+  h.fv_pp = vo;
+  h.cmacs_pp = cm;
   // cells, descriptors and child maps
+  std::vector<int> cells, cmap;
+  std::vector<Desc> desc;
+  std::vector<int> pos((size_t)nx * ny, -1);
   const int di[5] = {0, -1, 1, 0, 0}, dj[5] = {0, 0, 0, -1, 1};
+  long long cnt = 0, sum = 0;
   for (int k = 0; k < nn; ++k) {
-    const HNode& x = t.nodes[k];
+    const HNode& x = t[k];
     Node& n = dn[k];
+    cnt += n.nI;
+    for (int c : x.I) sum += c;
     n.cells = (int)cells.size();
     cells.insert(cells.end(), x.I.begin(), x.I.end());
     cells.insert(cells.end(), x.B.begin(), x.B.end());
@@ -803,7 +872,7 @@ static int analyse(cev_nd_precond_s* h, bool upload_all, size_t* n_nodes = nullp
       n.cmap[s] = -1;
       if (x.child[s] < 0) continue;
       n.cmap[s] = (int)cmap.size();
-      for (int cell : t.nodes[x.child[s]].B) {
+      for (int cell : t[x.child[s]].B) {
         const int p = pos[cell];
         if (p < 0) {
           set_error("nested dissection: a child's boundary cell is outside its parent's front");
@@ -815,31 +884,35 @@ static int analyse(cev_nd_precond_s* h, bool upload_all, size_t* n_nodes = nullp
     for (int c : x.I) pos[c] = -1;
     for (int c : x.B) pos[c] = -1;
   }
+  const long long nc = (long long)nx * ny;
+  h.cover[0] = cnt - nc;
+  h.cover[1] = sum - nc * (nc - 1) / 2;
+  h.n_nodes = dn.size();
+  h.n_desc = desc.size();
   // work lists per depth
-  for (int d = 0; d < h->ndepth; ++d) {
-    Level& L = h->levels[d];
+  for (int d = 0; d < h.ndepth; ++d) {
+    Level& L = h.levels[d];
     for (int k : by_depth[d]) {
       const Node& n = dn[k];
       const int f = n.nI + n.nB;
-      L.max_f = std::max(L.max_f, f);
-      L.max_nI = std::max(L.max_nI, n.nI);
-      const int nch = (f + TILE - 1) / TILE;
-      if (f <= SMALL_F) {
+      if (n.small) {
         L.small.push_back(k);
         L.max_f_small = std::max(L.max_f_small, f);
-      } else {
-        L.large.push_back(k);
-        L.max_nI_large = std::max(L.max_nI_large, n.nI);
-        for (int s = 0; s < 2; ++s)
-          if (n.child[s] >= 0)
-            for (int r = 0; r < dn[n.child[s]].nB; ++r) L.ext[s].push_back(make_int2(k, r));
-        for (int c = 0; c < nch; ++c) L.panel.push_back(make_int2(k, c));
-        for (int c = 0; c < nch * nch; ++c) L.tiles.push_back(make_int2(k, c));
-        for (int c = 0; c < (n.nB + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.gemv.push_back(make_int2(k, c));
+        continue;
       }
+      L.large.push_back(k);
+      L.max_f_large = std::max(L.max_f_large, f);
+      L.max_nI_large = std::max(L.max_nI_large, n.nI);
+      const int nch = (f + TILE - 1) / TILE;
+      for (int s = 0; s < 2; ++s)
+        if (n.child[s] >= 0)
+          for (int r = 0; r < dn[n.child[s]].nB; ++r) L.ext[s].push_back(make_int2(k, r));
+      for (int c = 0; c < nch; ++c) L.panel.push_back(make_int2(k, c));
+      for (int c = 0; c < nch * nch; ++c) L.tiles.push_back(make_int2(k, c));
+      for (int c = 0; c < (n.nB + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.gemv.push_back(make_int2(k, c));
       for (int c = 0; c < (n.nI + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.bwd.push_back(make_int2(k, c));
     }
-    if (!upload_all) continue;
+    if (!to_device) continue;
     int rc;
     if ((rc = upload(&L.d_small, L.small)) || (rc = upload(&L.d_large, L.large)) ||
         (rc = upload(&L.d_ext[0], L.ext[0])) || (rc = upload(&L.d_ext[1], L.ext[1])) ||
@@ -847,41 +920,79 @@ static int analyse(cev_nd_precond_s* h, bool upload_all, size_t* n_nodes = nullp
         (rc = upload(&L.d_gemv, L.gemv)) || (rc = upload(&L.d_bwd, L.bwd)))
       return rc;
   }
-  if (n_nodes) *n_nodes = dn.size();
-  if (n_desc) *n_desc = desc.size();
-  if (cover) {
-    // every cell eliminated exactly once: sum over nodes of the cell ids of I
-    // must equal 0 + 1 + ... + (n - 1), and the count must be n
-    long long sum = 0, cnt = 0;
-    for (const auto& x : t.nodes) {
-      cnt += (long long)x.I.size();
-      for (int c : x.I) sum += c;
-    }
-    const long long n = (long long)h->nx * h->ny;
-    cover[0] = cnt - n;
-    cover[1] = sum - n * (n - 1) / 2;
-  }
-  if (!upload_all) return CEV_OK;
+  if (!to_device) return CEV_OK;
+  CEV_CUDA(cudaGetDevice(&h.device));
   int rc;
-  if ((rc = upload(&h->d_nodes, dn)) || (rc = upload(&h->d_cells, cells)) ||
-      (rc = upload(&h->d_cmap, cmap)) || (rc = upload(&h->d_desc, desc)))
+  if ((rc = upload(&h.d_nodes, dn)) || (rc = upload(&h.d_cells, cells)) ||
+      (rc = upload(&h.d_cmap, cmap)) || (rc = upload(&h.d_desc, desc)))
     return rc;
   return CEV_OK;
 }
 
+// Shapes of the current device, the most recent few kept (a handle keeps its own).
+static int get_shape(int nx, int ny, std::shared_ptr<Shape>& out) {
+  static std::mutex mu;
+  static std::vector<std::shared_ptr<Shape>> cache;
+  int dev = 0;
+  CEV_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  for (size_t k = 0; k < cache.size(); ++k)
+    if (cache[k]->nx == nx && cache[k]->ny == ny && cache[k]->device == dev) {
+      out = cache[k];
+      std::rotate(cache.begin(), cache.begin() + k, cache.begin() + k + 1);  // most recent first
+      return CEV_OK;
+    }
+  auto s = std::make_shared<Shape>();
+  const int rc = analyse(*s, nx, ny, true);
+  if (rc != CEV_OK) return rc;
+  cache.insert(cache.begin(), s);
+  if (cache.size() > 4) cache.pop_back();
+  out = s;
+  return CEV_OK;
+}
+
+}  // namespace nd
+}  // namespace cev
+
+using namespace cev;
+using namespace cev::nd;
+
+struct cev_nd_precond_s {
+  int nx = 0, ny = 0, batch = 0, pol = 0, transpose = 0, device = 0;
+  double shift = 0;
+  size_t n = 0;
+  std::shared_ptr<Shape> shape;
+  float2* fac = nullptr;
+  float2* sar[2] = {nullptr, nullptr};
+  float2* fv = nullptr;
+  int* fault = nullptr;
+  const cev_fdfd_plan_s* plan = nullptr;
+  ~cev_nd_precond_s() {
+    cudaFree(fac); cudaFree(sar[0]); cudaFree(sar[1]); cudaFree(fv); cudaFree(fault);
+  }
+};
+
+namespace cev {
+namespace nd {
+
 static Args make_args(const cev_nd_precond_s* h, const Op& op) {
+  const Shape& S = *h->shape;
   Args a;
   a.op = op;
-  a.nodes = h->d_nodes;
-  a.cells = h->d_cells;
-  a.cmap = h->d_cmap;
-  a.desc = h->d_desc;
+  a.nodes = S.d_nodes;
+  a.cells = S.d_cells;
+  a.cmap = S.d_cmap;
+  a.desc = S.d_desc;
   a.fac = h->fac;
   a.sar[0] = h->sar[0];
   a.sar[1] = h->sar[1];
   a.fv = h->fv;
   a.fault = h->fault;
   a.n = h->n;
+  a.fac_pp = S.fac_pp;
+  a.sa_pp[0] = S.sa_pp[0];
+  a.sa_pp[1] = S.sa_pp[1];
+  a.fv_pp = S.fv_pp;
   return a;
 }
 
@@ -895,22 +1006,22 @@ static int launch_small(const Args& a, const Level& L, int B, cudaStream_t s) {
   return CEV_OK;
 }
 
+static unsigned zero_grid(long long elems) {
+  return (unsigned)std::max<long long>(1, std::min<long long>((elems + 255) / 256, 16LL * sm_count()));
+}
+
 static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
   const Args a = make_args(h, op);
+  const Shape& S = *h->shape;
   const int B = h->batch;
   CEV_CUDA(cudaMemsetAsync(h->fault, 0, sizeof(int), s));
-  long long fac_base = 0;
-  std::vector<long long> base(h->ndepth);
-  for (int d = 0; d < h->ndepth; ++d) {
-    base[d] = fac_base;
-    fac_base += h->levels[d].fac_stride * B;
-  }
-  for (int d = h->ndepth - 1; d >= 0; --d) {
-    const Level& L = h->levels[d];
+  for (int d = S.ndepth - 1; d >= 0; --d) {
+    const Level& L = S.levels[d];
     if (!L.large.empty()) {
-      CEV_CUDA(cudaMemsetAsync(h->fac + base[d], 0, sizeof(float2) * L.fac_stride * B, s));
-      if (L.s_stride > 0)
-        CEV_CUDA(cudaMemsetAsync(h->sar[d & 1], 0, sizeof(float2) * L.s_stride * B, s));
+      k_zero<<<zero_grid(L.fac_len * B), 256, 0, s>>>(h->fac, S.fac_pp, L.fac_lo, L.fac_len, B);
+      if (L.s_len > 0)
+        k_zero<<<zero_grid(L.s_len * B), 256, 0, s>>>(h->sar[d & 1], S.sa_pp[d & 1], 0, L.s_len, B);
+      CEV_CHECK_LAUNCH("nd zero");
     }
     if (!L.small.empty()) {
       int rc;
@@ -927,7 +1038,7 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
         k_extend<<<dim3((unsigned)L.ext[sl].size(), B), 128, 0, s>>>(a, L.d_ext[sl], sl);
     CEV_CHECK_LAUNCH("nd assemble");
     for (int k0 = 0; k0 < L.max_nI_large; k0 += NB) {
-      k_pivblock<<<dim3(nl, B), 256, 0, s>>>(a, L.d_large, k0);
+      k_pivblock<<<dim3((nl + 3) / 4, B), 128, 0, s>>>(a, L.d_large, (int)nl, k0);
       k_rowpanel<<<dim3((unsigned)L.panel.size(), B), 256, 0, s>>>(a, L.d_panel, k0);
       k_update<<<dim3((unsigned)L.tiles.size(), B), 128, 0, s>>>(a, L.d_tiles, k0);
       k_colpanel<<<dim3((unsigned)L.panel.size(), B), 256, 0, s>>>(a, L.d_panel, k0);
@@ -942,34 +1053,42 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
 int nd_apply(cev_nd_precond_s* h, const float2* v, float2* z, const double* sc, int sc_stride,
              int sc_index, const KState* st, cudaStream_t s) {
   Op op{};  // entries are not needed by the apply kernels
-  const Args a = nd::make_args(h, op);
+  const nd::Args a = nd::make_args(h, op);
+  const nd::Shape& S = *h->shape;
   nd::ApplyIO io{v, z, sc, sc_stride, sc_index, st};
   const int B = h->batch;
   int rc;
-  for (int d = h->ndepth - 1; d >= 0; --d) {
-    const nd::Level& L = h->levels[d];
+  for (int d = S.ndepth - 1; d >= 0; --d) {
+    const nd::Level& L = S.levels[d];
     if (!L.small.empty()) {
-      const int bytes = L.max_f_small * (int)sizeof(float2);
-      nd::k_fwd<true><<<dim3((unsigned)L.small.size(), B), 256, bytes, s>>>(a, io, L.d_small);
+      const unsigned ns = (unsigned)L.small.size();
+      nd::k_fwd_small<<<dim3((ns + nd::WPB - 1) / nd::WPB, B), nd::WPB * 32, 0, s>>>(
+          a, io, L.d_small, (int)ns);
     }
     if (!L.large.empty()) {
-      const int bytes = L.max_f * (int)sizeof(float2);
-      if ((rc = allow_dynamic_smem((const void*)nd::k_fwd<false>, bytes)) != CEV_OK) return rc;
-      nd::k_fwd<false><<<dim3((unsigned)L.large.size(), B), 256, bytes, s>>>(a, io, L.d_large);
+      const int bytes = L.max_f_large * (int)sizeof(float2);
+      if ((rc = allow_dynamic_smem((const void*)nd::k_fwd_large, bytes)) != CEV_OK) return rc;
+      nd::k_fwd_large<<<dim3((unsigned)L.large.size(), B), 256, bytes, s>>>(a, io, L.d_large);
       if (!L.gemv.empty()) {
-        const int gb = L.max_nI * (int)sizeof(float2);
+        const int gb = L.max_nI_large * (int)sizeof(float2);
         if ((rc = allow_dynamic_smem((const void*)nd::k_fwd_gemv, gb)) != CEV_OK) return rc;
         nd::k_fwd_gemv<<<dim3((unsigned)L.gemv.size(), B), 256, gb, s>>>(a, io, L.d_gemv);
       }
     }
     CEV_CHECK_LAUNCH("nd forward");
   }
-  for (int d = 0; d < h->ndepth; ++d) {
-    const nd::Level& L = h->levels[d];
-    if (L.bwd.empty()) continue;
-    const int bytes = L.max_f * (int)sizeof(float2);
-    if ((rc = allow_dynamic_smem((const void*)nd::k_bwd, bytes)) != CEV_OK) return rc;
-    nd::k_bwd<<<dim3((unsigned)L.bwd.size(), B), 256, bytes, s>>>(a, io, L.d_bwd);
+  for (int d = 0; d < S.ndepth; ++d) {
+    const nd::Level& L = S.levels[d];
+    if (!L.bwd.empty()) {
+      const int bytes = L.max_f_large * (int)sizeof(float2);
+      if ((rc = allow_dynamic_smem((const void*)nd::k_bwd_large, bytes)) != CEV_OK) return rc;
+      nd::k_bwd_large<<<dim3((unsigned)L.bwd.size(), B), 256, bytes, s>>>(a, io, L.d_bwd);
+    }
+    if (!L.small.empty()) {
+      const unsigned ns = (unsigned)L.small.size();
+      nd::k_bwd_small<<<dim3((ns + nd::WPB - 1) / nd::WPB, B), nd::WPB * 32, 0, s>>>(
+          a, io, L.d_small, (int)ns);
+    }
     CEV_CHECK_LAUNCH("nd backward");
   }
   return CEV_OK;
@@ -1012,12 +1131,14 @@ int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double*
   h->n = plan->n();
   h->plan = plan;
   cudaGetDevice(&h->device);
-  int rc = nd::analyse(h, true);
   auto fail = [&](int code) {
     delete h;
     return code;
   };
+  int rc = nd::get_shape(plan->nx, plan->ny, h->shape);
   if (rc != CEV_OK) return fail(rc);
+  const Shape& S = *h->shape;
+  const size_t B = (size_t)h->batch;
   auto alloc = [&](float2** p, size_t elems) -> int {
     if (elems == 0) return CEV_OK;
     const cudaError_t e = cudaMalloc((void**)p, sizeof(float2) * elems);
@@ -1029,8 +1150,8 @@ int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double*
     }
     return CEV_OK;
   };
-  if ((rc = alloc(&h->fac, h->fac_elems)) || (rc = alloc(&h->sar[0], h->sar_elems[0])) ||
-      (rc = alloc(&h->sar[1], h->sar_elems[1])) || (rc = alloc(&h->fv, h->fv_elems)))
+  if ((rc = alloc(&h->fac, (size_t)S.fac_pp * B)) || (rc = alloc(&h->sar[0], (size_t)S.sa_pp[0] * B)) ||
+      (rc = alloc(&h->sar[1], (size_t)S.sa_pp[1] * B)) || (rc = alloc(&h->fv, (size_t)S.fv_pp * B)))
     return fail(rc);
   if (cudaMalloc((void**)&h->fault, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
@@ -1042,15 +1163,16 @@ int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double*
             eps_shared ? (size_t)0 : plan->n(), eps, plan->cx32[tr], plan->cy32[tr],
             plan->k2_32, (float)shift};
   if ((rc = nd::factor(h, op, stream)) != CEV_OK) return fail(rc);
-  // the Schur arenas are only needed during the factorisation
   cudaError_t e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return fail(cuda_status(e, "direct preconditioner factorisation"));
   int fault = 0;
-  cudaMemcpy(&fault, h->fault, sizeof(int), cudaMemcpyDeviceToHost);
+  e = cudaMemcpy(&fault, h->fault, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(cuda_status(e, "direct preconditioner fault flag"));
   if (fault) {
     set_error("direct preconditioner: a zero or non-finite pivot in the complex64 factorisation");
     return fail(CEV_ERR_NUMERIC);
   }
+  // the Schur arenas are only needed during the factorisation
   cudaFree(h->sar[0]);
   cudaFree(h->sar[1]);
   h->sar[0] = h->sar[1] = nullptr;
@@ -1066,9 +1188,9 @@ int cev_nd_precond_apply(cev_nd_precond h, const void* v, void* z, cudaStream_t 
 int cev_nd_precond_info(cev_nd_precond h, size_t* factor_bytes, double* factor_cmacs,
                         int* depths) {
   CEV_REQUIRE(h != nullptr, "NULL handle");
-  if (factor_bytes) *factor_bytes = sizeof(float2) * h->fac_elems;
-  if (factor_cmacs) *factor_cmacs = h->flops;
-  if (depths) *depths = h->ndepth;
+  if (factor_bytes) *factor_bytes = sizeof(float2) * (size_t)h->shape->fac_pp * h->batch;
+  if (factor_cmacs) *factor_cmacs = h->shape->cmacs_pp * h->batch;
+  if (depths) *depths = h->shape->ndepth;
   return CEV_OK;
 }
 
@@ -1076,20 +1198,17 @@ int cev_nd_analyse(int nx, int ny, size_t* n_nodes, int* depths, size_t* factor_
                    double* factor_cmacs, size_t* n_desc, long long* cover) {
   CEV_REQUIRE(nx >= 2 && ny >= 2 && (size_t)nx * ny < ((size_t)1 << 31), "bad grid %d x %d", nx,
               ny);
-  cev_nd_precond_s h;
-  h.nx = nx;
-  h.ny = ny;
-  h.batch = 1;
-  h.n = (size_t)nx * ny;
-  long long cv[2] = {0, 0};
-  const int rc = nd::analyse(&h, false, n_nodes, n_desc, cv);
+  nd::Shape h;
+  const int rc = nd::analyse(h, nx, ny, false);
   if (rc != CEV_OK) return rc;
+  if (n_nodes) *n_nodes = h.n_nodes;
   if (depths) *depths = h.ndepth;
-  if (factor_elems) *factor_elems = h.fac_elems;
-  if (factor_cmacs) *factor_cmacs = h.flops;
+  if (factor_elems) *factor_elems = (size_t)h.fac_pp;
+  if (factor_cmacs) *factor_cmacs = h.cmacs_pp;
+  if (n_desc) *n_desc = h.n_desc;
   if (cover) {
-    cover[0] = cv[0];
-    cover[1] = cv[1];
+    cover[0] = h.cover[0];
+    cover[1] = h.cover[1];
   }
   return CEV_OK;
 }

@@ -70,13 +70,27 @@ __device__ __forceinline__ T ldx(const T* p) {
     return __ldg(p);
 }
 
+// Input conversion of the stencil: a complex64 vector may feed the FP64
+// stencil (the exact operator applied to a complex64 preconditioned vector).
+template <typename C, typename X>
+struct CvtIn;
+template <typename C>
+struct CvtIn<C, C> {
+  static __device__ __forceinline__ C go(C v) { return v; }
+};
+template <>
+struct CvtIn<double2, float2> {
+  static __device__ __forceinline__ double2 go(float2 v) { return to_d(v); }
+};
+
 // Sliding-window row iterator over one column j for rows [i0, i1).
 // Calls ep(i, Au, u_c) for every row with Au the stencil (without output
 // scaling) and u_c the centre value.  E is the permittivity element: R (real
 // eps) or Cplx<R> (complex eps, lossy media).
-template <typename R, int POL, typename Epi, bool CG = false, typename E = R>
+template <typename R, int POL, typename Epi, bool CG = false, typename E = R,
+          typename X = Cplx<R>>
 __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, int i1,
-                                               const Cplx<R>* x,
+                                               const X* x,
                                                const E* __restrict__ eps,
                                                const Coef<R>* __restrict__ cx,
                                                const Coef<R>& cyj, R k2, Epi& ep) {
@@ -85,8 +99,8 @@ __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, in
   const int jp = (j == ny - 1) ? 0 : j + 1;
   const int jmm = (jm == 0) ? ny - 1 : jm - 1;
   const int im0 = (i0 == 0) ? nx - 1 : i0 - 1;
-  C u_m = ldx<CG>(x + (size_t)im0 * ny + j);
-  C u_c = ldx<CG>(x + (size_t)i0 * ny + j);
+  C u_m = CvtIn<C, X>::go(ldx<CG>(x + (size_t)im0 * ny + j));
+  C u_c = CvtIn<C, X>::go(ldx<CG>(x + (size_t)i0 * ny + j));
   // Hz: eps window along i (for d_yy) ; Ez: unused
   E e_m{}, dyy_m{};
   if (POL == POL_HZ) {
@@ -98,9 +112,9 @@ __device__ __forceinline__ void stencil_column(int nx, int ny, int j, int i0, in
   for (int i = i0; i < i1; ++i) {
     const int ip = (i == nx - 1) ? 0 : i + 1;
     const size_t row = (size_t)i * ny;
-    const C u_p = ldx<CG>(x + (size_t)ip * ny + j);
-    const C u_l = ldx<CG>(x + row + jm);
-    const C u_r = ldx<CG>(x + row + jp);
+    const C u_p = CvtIn<C, X>::go(ldx<CG>(x + (size_t)ip * ny + j));
+    const C u_l = CvtIn<C, X>::go(ldx<CG>(x + row + jm));
+    const C u_r = CvtIn<C, X>::go(ldx<CG>(x + row + jp));
     const Coef<R> c = cx[i];
     C acc;
     if (POL == POL_EZ) {
