@@ -60,7 +60,7 @@ int allow_dynamic_smem(const void* fn, int bytes, int carveout) {
 }
 
 // ------------------------------------------------------------ PML profiles
-// sig_w / s_value of ceviche/derivatives.py:219-226 (m = 3, lnR = -30)
+// sig_w / s_value of ceviche/derivatives.py:209-216 (m = 3, lnR = -30)
 static zd s_value(double l, double dw, double omega) {
   const double ETA_0 = std::sqrt(MU_0 / EPSILON_0);
   const double m = 3.0, lnR = -30.0;

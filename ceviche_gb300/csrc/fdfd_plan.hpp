@@ -14,7 +14,7 @@ using zd = std::complex<double>;
 constexpr double EPSILON_0 = 8.85418782e-12;
 constexpr double MU_0 = 1.25663706e-6;
 
-// 1D stretch profile s(i) of ceviche/derivatives.py:183-226 ('f': offset 0.5,
+// 1D stretch profile s(i) of ceviche/derivatives.py:173-216 ('f': offset 0.5,
 // 'b': offset 1); returns s itself (not 1/s).
 std::vector<zd> sfactor(bool forward, double omega, double dL, int N, int npml);
 

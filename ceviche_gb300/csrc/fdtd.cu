@@ -8,7 +8,7 @@
 //   mDz0*dt = (1+aDx)(1+aDy), mDz1 = (1-aDx-aDy-aDx aDy)/((1+aDx)(1+aDy)),
 //   mDz2*CHz = S/((1+aDx)(1+aDy)) CH',  mDz4 = -4 aDx aDy/((1+aDx)(1+aDy))
 // with dEy = Ez[i,j+1]-Ez, dEx' = -(Ez[i+1,j]-Ez), CH' = (Hy-Hy[i-1])-(Hx-Hx[i,j-1])
-// (the curls of ceviche/derivatives.py:26-40 without the 1/dL factor, which
+// (the curls of ceviche/derivatives.py:16-30 without the 1/dL factor, which
 // sits in S).  mHx4, mHy4 and mDz3 carry sigma_z and are exactly zero, so the
 // IHx, IHy and ICHz integrals never reach a field.  The PML integrals are
 // accumulated only where their coefficient is non-zero; elsewhere they are

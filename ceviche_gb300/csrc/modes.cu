@@ -6,7 +6,7 @@
 // batch of 1D cross sections, one CTA per section.
 //
 // Dxf Dxb is the 1D second difference of ceviche/derivatives.py with its
-// SC-PML stretch (sfactor, derivatives.py:183-226) and the periodic wrap of
+// SC-PML stretch (sfactor, derivatives.py:173-216) and the periodic wrap of
 // the (N, 1) grid: row i holds up_i at column i+1, dn_i at column i-1
 // (indices mod N) and -(up_i + dn_i) on the diagonal, with
 // up_i = 1 / (s_f[i] s_b[i+1] (k0 dL)^2) and dn_i = 1 / (s_f[i] s_b[i] (k0 dL)^2).

@@ -5,7 +5,7 @@
 //     (A_axis u)_i = P_i [ W_{i+1/2} (R_{i+1} f+ u_{i+1} - R_i u_i)
 //                         - W_{i-1/2} (R_i u_i - R_{i-1} f- u_{i-1}) ]
 // with the periodic wrap carrying the Bloch phasor f+ = ph at i = N-1 and
-// f- = conj(ph) at i = 0 (ceviche/derivatives.py:104-134):
+// f- = conj(ph) at i = 0 (ceviche/derivatives.py:94-124):
 //   Ez: P = 1/s_f, W_{i+1/2} = 1/s_b[i+1], R = 1, overall sign -1
 //       (-(1/mu0) Dxf Dxb, ceviche/fdfd.py:174-175)
 //   Hz: P = 1/s_b, W_{i+1/2} = (1/s_f[i]) * d[i], R = 1, sign +1, where d is

@@ -65,7 +65,7 @@ typedef struct cev_fdfd_plan_s* cev_fdfd_plan;
 /*
  * Precomputes the SC-PML stencil coefficient tables of `batch` problems that
  * share a grid and differ in omega.  Replaces the per-solve sparse assembly of
- * ceviche/derivatives.py:44-226 (compute_derivative_matrices, create_S_matrices,
+ * ceviche/derivatives.py:34-216 (compute_derivative_matrices, create_S_matrices,
  * create_sfactor, s_value) and ceviche/fdfd.py:80-112 (_setup_derivatives,
  * Bloch phases).  omegas is a HOST array of length batch.
  */

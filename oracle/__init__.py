@@ -14,8 +14,8 @@ so the reference's VJP rules are restated in ``oracle.fdfd`` / ``oracle.fdtd``).
 
 Modules:
     constants  -- ceviche/constants.py:7-11
-    fdfd       -- ceviche/derivatives.py:44-226, ceviche/fdfd.py:58-244,
+    fdfd       -- ceviche/derivatives.py:34-216, ceviche/fdfd.py:58-244,
                   ceviche/primitives.py:103-148, ceviche/solvers.py:50-62
-    fdtd       -- ceviche/fdtd.py:74-316, ceviche/derivatives.py:26-40,
+    fdtd       -- ceviche/fdtd.py:74-316, ceviche/derivatives.py:16-30,
                   ceviche/utils.py:153-176
 """

@@ -1,8 +1,8 @@
 """FP64 CPU restatement of ceviche's FDFD path -- TEST INFRASTRUCTURE ONLY.
 
 Restates (own code, same arithmetic):
-    * PML stretch factors       ceviche/derivatives.py:183-226
-    * derivative matrices       ceviche/derivatives.py:44-134 (incl. 1D case :85-89)
+    * PML stretch factors       ceviche/derivatives.py:173-216
+    * derivative matrices       ceviche/derivatives.py:34-124 (incl. 1D case :75-78)
     * Ez / Hz system matrices   ceviche/fdfd.py:172-185, :200-233
     * direct solve              ceviche/primitives.py:103-119 -> solvers.py:50-62
                                 (scipy SuperLU ``spsolve``; PARDISO is optional
@@ -24,18 +24,18 @@ from .constants import EPSILON_0, MU_0, ETA_0
 
 # ---------------------------------------------------------------- PML profiles
 def sig_w(l, dw, m=3, lnR=-30):
-    """ceviche/derivatives.py:219-222."""
+    """ceviche/derivatives.py:209-212."""
     sig_max = -(m + 1) * lnR / (2 * ETA_0 * dw)
     return sig_max * (l / dw) ** m
 
 
 def s_value(l, dw, omega):
-    """ceviche/derivatives.py:224-226."""
+    """ceviche/derivatives.py:214-216."""
     return 1 - 1j * sig_w(l, dw) / (omega * EPSILON_0)
 
 
 def sfactor(direction, omega, dL, N, npml):
-    """1D stretch profile, ceviche/derivatives.py:183-217.
+    """1D stretch profile, ceviche/derivatives.py:173-207.
 
     'f': i <= npml -> l = dL*(npml - i + 0.5); i > N - npml -> l = dL*(i - (N - npml) - 0.5)
     'b': same with offsets 1 instead of 0.5.
@@ -56,7 +56,7 @@ def sfactor(direction, omega, dL, N, npml):
 # --------------------------------------------------------- derivative matrices
 def _d1(direction, n, dL, phase):
     """1D difference matrix with Bloch phasor on the wrap entry
-    (ceviche/derivatives.py:104-134)."""
+    (ceviche/derivatives.py:94-124)."""
     ph = np.exp(1j * phase)
     if direction == "f":
         D = sp.diags([-1, 1, ph], [0, 1, -n + 1], shape=(n, n), dtype=np.complex128)
@@ -67,7 +67,7 @@ def _d1(direction, n, dL, phase):
 
 def derivative_matrices(omega, shape, npml, dL, bloch_x=0.0, bloch_y=0.0):
     """(Dxf, Dxb, Dyf, Dyb) with the S-factors folded in as row scalings
-    (ceviche/derivatives.py:44-69, 139-181).  Flat index = i*Ny + j."""
+    (ceviche/derivatives.py:34-59, 129-171).  Flat index = i*Ny + j."""
     Nx, Ny = shape
     Ix, Iy = sp.eye(Nx), sp.eye(Ny)
     out = []

@@ -6,7 +6,7 @@ Restates (own code, same arithmetic and operation order):
     * update coefficients ceviche/fdtd.py:265-316
     * eps averaging      ceviche/utils.py:153-176  (xx along axis 0, yy along axis 1)
     * one step           ceviche/fdtd.py:74-144 with the curls of
-                         ceviche/derivatives.py:26-40 (periodic roll)
+                         ceviche/derivatives.py:16-30 (periodic roll)
 
 The reference stores (Nx, Ny, 1) arrays; with Nz == 1 every roll along z is
 the identity, so the z-differences are exactly zero and the arrays here are
@@ -126,7 +126,7 @@ class FDTD2D:
             self.te_active = True
         Ex, Ey, Ez = f["Ex"], f["Ey"], f["Ez"]
         roll = np.roll
-        # curl E (derivatives.py:26-32); z-rolls are the identity for Nz == 1
+        # curl E (derivatives.py:16-22); z-rolls are the identity for Nz == 1
         CEx = (roll(Ez, -1, axis=1) - Ez) / dL - (Ey - Ey) / dL
         CEy = (Ex - Ex) / dL - (roll(Ez, -1, axis=0) - Ez) / dL
         a["ICEx"] = a["ICEx"] + CEx
@@ -142,7 +142,7 @@ class FDTD2D:
             f["Hz"] = c["mHz1"] * f["Hz"] + c["mHz2"] * CEz + c["mHz3"] * a["ICEz"] + c["mHz4"] * a["IHz"]
         f["Hx"], f["Hy"] = Hx, Hy
         Hz = f["Hz"]
-        # curl H (derivatives.py:34-40)
+        # curl H (derivatives.py:24-30)
         CHz = (Hy - roll(Hy, 1, axis=0)) / dL - (Hx - roll(Hx, 1, axis=1)) / dL
         a["ICHz"] = a["ICHz"] + CHz
         a["IDz"] = a["IDz"] + f["Dz"]
