@@ -71,6 +71,8 @@ struct Node {
   int desc, ndesc;   // original-entry descriptors
   int par;           // Schur arena of this node's depth (depth & 1)
   int small;         // f <= SMALL_F
+  int lidx;          // large fronts: index in its depth's list of large fronts
+  int pad;
   long long top;     // [G | H] (nI x f), offset within one problem's factor block
   long long bl;      // -K (nB x nI)
   long long s;       // S (nB x nB, row-major) within one problem's block of arena par
@@ -105,6 +107,7 @@ struct Args {
   float2* sar[2];
   float2* fv;
   int* fault;  // set when a pivot is zero or not finite
+  float2* lub; // LU factors of the current pivot blocks [B][large fronts][NB][NB]
   size_t n;    // cells per problem
   long long fac_pp, sa_pp[2], fv_pp;  // per-problem strides
 };
@@ -348,11 +351,16 @@ __device__ __forceinline__ float2 shfl2(float2 v, int src) {
   return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
-// In-place inverse of the pivot block F[k0:k0+nb, k0:k0+nb], one warp per
-// (node, problem): lane j holds column j in registers (padded with the
-// identity to 32 x 32), Gauss-Jordan with the pivot column broadcast by shuffles.
+// Pivot block of a block step, one warp per (large front, problem): the LU
+// factors (no pivoting) of A_pp = F[k0:k0+nb, k0:k0+nb], padded with the
+// identity to NB x NB, go to the scratch `lub` for the two panel kernels, and
+// the explicit inverse replaces A_pp in the front.  The panels are then
+// formed by triangular solves with these factors, not by products with the
+// explicit inverse: on Helmholtz fronts the explicit-inverse form loses about
+// two orders of magnitude of accuracy in complex64.
 __global__ void __launch_bounds__(128) k_pivblock(Args a, const int* __restrict__ list, int count,
                                                   int k0) {
+  __shared__ float2 blk[4][NB][NB + 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x * 4 + warp;
   if (item >= count) return;
@@ -361,66 +369,83 @@ __global__ void __launch_bounds__(128) k_pivblock(Args a, const int* __restrict_
   const int b = blockIdx.y;
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
   float2* base = ftop(a, n, b);
-  float2 reg[NB];
-#pragma unroll
+  float2(*B)[NB + 1] = blk[warp];
   for (int r = 0; r < NB; ++r)
-    reg[r] = (r < nb && lane < nb) ? base[(size_t)(k0 + r) * f + k0 + lane]
-                                   : make_float2(r == lane ? 1.f : 0.f, 0.f);
-#pragma unroll
-  for (int p = 0; p < NB; ++p) {
-    const float2 d = shfl2(reg[p], p);
-    if (p < nb && lane == 0) check_pivot(a, d);
-    const float2 pinv = crcp(d);
-    const float2 rp = cmul(reg[p], pinv);  // this lane's entry of the scaled pivot row
-#pragma unroll
-    for (int r = 0; r < NB; ++r) {
-      if (r == p) continue;
-      const float2 c = shfl2(reg[r], p);  // pivot column entry of row r
-      if (lane == p) {
-        const float2 t = cmul(c, pinv);
-        reg[r] = make_float2(-t.x, -t.y);
-      } else {
-        reg[r] = csub(reg[r], cmul(c, rp));
-      }
+    B[r][lane] = (r < nb && lane < nb) ? base[(size_t)(k0 + r) * f + k0 + lane]
+                                       : make_float2(r == lane ? 1.f : 0.f, 0.f);
+  __syncwarp();
+  // LU without pivoting, lane j owns column j
+  for (int k = 0; k < NB; ++k) {
+    const float2 piv = B[k][k];
+    if (k < nb && lane == 0) check_pivot(a, piv);
+    const float2 pinv = crcp(piv);
+    if (lane > k) B[lane][k] = cmul(B[lane][k], pinv);
+    __syncwarp();
+    if (lane > k) {
+      const float2 ukj = B[k][lane];
+      for (int r = k + 1; r < NB; ++r) B[r][lane] = csub(B[r][lane], cmul(B[r][k], ukj));
     }
-    reg[p] = (lane == p) ? pinv : rp;
+    __syncwarp();
+  }
+  float2* lu = a.lub + ((size_t)b * count + n.lidx) * NB * NB;
+  for (int r = 0; r < NB; ++r) lu[r * NB + lane] = B[r][lane];
+  // column `lane` of A_pp^-1 = U^-1 L^-1 e_lane
+  float2 y[NB];
+#pragma unroll
+  for (int r = 0; r < NB; ++r) {
+    float2 t = make_float2(r == lane ? 1.f : 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < r; ++k) t = csub(t, cmul(B[r][k], y[k]));
+    y[r] = t;
+  }
+#pragma unroll
+  for (int r = NB - 1; r >= 0; --r) {
+    float2 t = y[r];
+#pragma unroll
+    for (int k = r + 1; k < NB; ++k) t = csub(t, cmul(B[r][k], y[k]));
+    y[r] = cmul(t, crcp(B[r][r]));
   }
   if (lane < nb)
 #pragma unroll
     for (int r = 0; r < NB; ++r)
-      if (r < nb) base[(size_t)(k0 + r) * f + k0 + lane] = reg[r];
+      if (r < nb) base[(size_t)(k0 + r) * f + k0 + lane] = y[r];
 }
 
-// Pivot rows: F[p, c] = Ainv F[p, c] for the 64 columns of one chunk outside
-// the pivot block (work: node index, column chunk).
-__global__ void __launch_bounds__(256) k_rowpanel(Args a, const int2* __restrict__ work, int k0) {
-  __shared__ float2 Ai[NB][NB + 1];
-  __shared__ float2 P[NB][TILE + 1];
+// Pivot rows: F[p, c] = U^-1 L^-1 F[p, c] for the 64 columns of one chunk
+// outside the pivot block, one thread per column (work: node index, column chunk).
+__global__ void __launch_bounds__(TILE) k_rowpanel(Args a, const int2* __restrict__ work, int k0,
+                                                   int count) {
+  __shared__ float2 LU[NB][NB + 1];
+  __shared__ float2 dinv[NB];
   const int2 w = work[blockIdx.x];
   const Node n = a.nodes[w.x];
   if (k0 >= n.nI) return;
   const int b = blockIdx.y;
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
-  const int c0 = w.y * TILE;
-  float2* base = ftop(a, n, b);
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int r = e / nb, c = e - r * nb;
-    Ai[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
-  }
-  for (int e = threadIdx.x; e < nb * TILE; e += blockDim.x) {
-    const int r = e / TILE, c = e - r * TILE;
-    const int gc = c0 + c;
-    P[r][c] = (gc < f) ? base[(size_t)(k0 + r) * f + gc] : make_float2(0.f, 0.f);
-  }
+  const float2* lu = a.lub + ((size_t)b * count + n.lidx) * NB * NB;
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) LU[e / NB][e % NB] = lu[e];
   __syncthreads();
-  for (int e = threadIdx.x; e < nb * TILE; e += blockDim.x) {
-    const int r = e / TILE, c = e - r * TILE;
-    const int gc = c0 + c;
-    if (gc >= f || (gc >= k0 && gc < k0 + nb)) continue;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int k = 0; k < nb; ++k) acc = cfma(Ai[r][k], P[k][c], acc);
-    base[(size_t)(k0 + r) * f + gc] = acc;
+  if (threadIdx.x < NB) dinv[threadIdx.x] = crcp(LU[threadIdx.x][threadIdx.x]);
+  __syncthreads();
+  const int c = w.y * TILE + threadIdx.x;
+  if (c >= f || (c >= k0 && c < k0 + nb)) return;
+  float2* base = ftop(a, n, b);
+  float2 x[NB];
+#pragma unroll
+  for (int r = 0; r < NB; ++r) x[r] = r < nb ? base[(size_t)(k0 + r) * f + c] : make_float2(0.f, 0.f);
+#pragma unroll
+  for (int r = 1; r < NB; ++r)
+#pragma unroll
+    for (int k = 0; k < r; ++k) x[r] = csub(x[r], cmul(LU[r][k], x[k]));
+#pragma unroll
+  for (int r = NB - 1; r >= 0; --r) {
+#pragma unroll
+    for (int k = r + 1; k < NB; ++k) x[r] = csub(x[r], cmul(LU[r][k], x[k]));
+    x[r] = cmul(x[r], dinv[r]);
   }
+#pragma unroll
+  for (int r = 0; r < NB; ++r)
+    if (r < nb) base[(size_t)(k0 + r) * f + c] = x[r];
 }
 
 // Rank-nb update of every entry outside the pivot rows and columns:
@@ -486,10 +511,12 @@ __global__ void __launch_bounds__(128) k_update(Args a, const int2* __restrict__
   }
 }
 
-// Pivot columns: F[r, p] = -F[r, p] Ainv for the 64 rows of one chunk
-// outside the pivot block (work: node index, row chunk).
-__global__ void __launch_bounds__(256) k_colpanel(Args a, const int2* __restrict__ work, int k0) {
-  __shared__ float2 Ai[NB][NB + 1];
+// Pivot columns: F[r, p] = -F[r, p] U^-1 L^-1 for the 64 rows of one chunk
+// outside the pivot block, one thread per row (work: node index, row chunk).
+__global__ void __launch_bounds__(TILE) k_colpanel(Args a, const int2* __restrict__ work, int k0,
+                                                   int count) {
+  __shared__ float2 LU[NB][NB + 1];
+  __shared__ float2 dinv[NB];
   __shared__ float2 P[TILE][NB + 1];
   const int2 w = work[blockIdx.x];
   const Node n = a.nodes[w.x];
@@ -497,24 +524,41 @@ __global__ void __launch_bounds__(256) k_colpanel(Args a, const int2* __restrict
   const int b = blockIdx.y;
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
   const int r0 = w.y * TILE;
-  const float2* base = ftop(a, n, b);
-  for (int e = threadIdx.x; e < nb * nb; e += blockDim.x) {
-    const int r = e / nb, c = e - r * nb;
-    Ai[r][c] = base[(size_t)(k0 + r) * f + k0 + c];
-  }
+  const float2* lu = a.lub + ((size_t)b * count + n.lidx) * NB * NB;
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) LU[e / NB][e % NB] = lu[e];
   for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
     const int i = e / NB, k = e - i * NB;
     const int r = r0 + i;
     P[i][k] = (r < f && k < nb) ? *fel(a, n, b, r, k0 + k) : make_float2(0.f, 0.f);
   }
   __syncthreads();
+  if (threadIdx.x < NB) dinv[threadIdx.x] = crcp(LU[threadIdx.x][threadIdx.x]);
+  __syncthreads();
+  const int i = threadIdx.x, r = r0 + i;
+  if (r < f && !(r >= k0 && r < k0 + nb)) {
+    float2 x[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) x[k] = P[i][k];
+    // x U = a (columns left to right), then x L = y (right to left)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+#pragma unroll
+      for (int k = 0; k < j; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
+      x[j] = cmul(x[j], dinv[j]);
+    }
+#pragma unroll
+    for (int j = NB - 2; j >= 0; --j)
+#pragma unroll
+      for (int k = j + 1; k < NB; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
+#pragma unroll
+    for (int k = 0; k < NB; ++k) P[i][k] = make_float2(-x[k].x, -x[k].y);
+  }
+  __syncthreads();
   for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
-    const int i = e / NB, k = e - i * NB;
-    const int r = r0 + i;
-    if (k >= nb || r >= f || (r >= k0 && r < k0 + nb)) continue;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int q = 0; q < nb; ++q) acc = cfma(P[i][q], Ai[q][k], acc);
-    *fel(a, n, b, r, k0 + k) = make_float2(-acc.x, -acc.y);
+    const int ii = e / NB, k = e - ii * NB;
+    const int rr = r0 + ii;
+    if (k >= nb || rr >= f || (rr >= k0 && rr < k0 + nb)) continue;
+    *fel(a, n, b, rr, k0 + k) = P[ii][k];
   }
 }
 
@@ -893,13 +937,15 @@ static int analyse(Shape& h, int nx, int ny, bool to_device) {
   for (int d = 0; d < h.ndepth; ++d) {
     Level& L = h.levels[d];
     for (int k : by_depth[d]) {
-      const Node& n = dn[k];
+      Node& n = dn[k];
       const int f = n.nI + n.nB;
+      n.lidx = -1;
       if (n.small) {
         L.small.push_back(k);
         L.max_f_small = std::max(L.max_f_small, f);
         continue;
       }
+      dn[k].lidx = (int)L.large.size();
       L.large.push_back(k);
       L.max_f_large = std::max(L.max_f_large, f);
       L.max_nI_large = std::max(L.max_nI_large, n.nI);
@@ -965,10 +1011,12 @@ struct cev_nd_precond_s {
   float2* fac = nullptr;
   float2* sar[2] = {nullptr, nullptr};
   float2* fv = nullptr;
+  float2* lub = nullptr;  // pivot-block LU scratch (factorisation only)
   int* fault = nullptr;
   const cev_fdfd_plan_s* plan = nullptr;
   ~cev_nd_precond_s() {
-    cudaFree(fac); cudaFree(sar[0]); cudaFree(sar[1]); cudaFree(fv); cudaFree(fault);
+    cudaFree(fac); cudaFree(sar[0]); cudaFree(sar[1]); cudaFree(fv); cudaFree(lub);
+    cudaFree(fault);
   }
 };
 
@@ -988,6 +1036,7 @@ static Args make_args(const cev_nd_precond_s* h, const Op& op) {
   a.sar[1] = h->sar[1];
   a.fv = h->fv;
   a.fault = h->fault;
+  a.lub = h->lub;
   a.n = h->n;
   a.fac_pp = S.fac_pp;
   a.sa_pp[0] = S.sa_pp[0];
@@ -1039,9 +1088,9 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
     CEV_CHECK_LAUNCH("nd assemble");
     for (int k0 = 0; k0 < L.max_nI_large; k0 += NB) {
       k_pivblock<<<dim3((nl + 3) / 4, B), 128, 0, s>>>(a, L.d_large, (int)nl, k0);
-      k_rowpanel<<<dim3((unsigned)L.panel.size(), B), 256, 0, s>>>(a, L.d_panel, k0);
+      k_rowpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
       k_update<<<dim3((unsigned)L.tiles.size(), B), 128, 0, s>>>(a, L.d_tiles, k0);
-      k_colpanel<<<dim3((unsigned)L.panel.size(), B), 256, 0, s>>>(a, L.d_panel, k0);
+      k_colpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
     }
     CEV_CHECK_LAUNCH("nd sweep");
   }
@@ -1153,6 +1202,10 @@ int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double*
   if ((rc = alloc(&h->fac, (size_t)S.fac_pp * B)) || (rc = alloc(&h->sar[0], (size_t)S.sa_pp[0] * B)) ||
       (rc = alloc(&h->sar[1], (size_t)S.sa_pp[1] * B)) || (rc = alloc(&h->fv, (size_t)S.fv_pp * B)))
     return fail(rc);
+  size_t max_large = 0;
+  for (const auto& L : S.levels) max_large = std::max(max_large, L.large.size());
+  if ((rc = alloc(&h->lub, max_large * B * NB * NB)))
+    return fail(rc);
   if (cudaMalloc((void**)&h->fault, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     set_error("direct preconditioner: cannot allocate its fault flag");
@@ -1176,6 +1229,8 @@ int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double*
   cudaFree(h->sar[0]);
   cudaFree(h->sar[1]);
   h->sar[0] = h->sar[1] = nullptr;
+  cudaFree(h->lub);
+  h->lub = nullptr;
   *out = h;
   return CEV_OK;
 }
