@@ -209,6 +209,21 @@ def fdfd_numbers():
            "us_per_iteration": 1e6 * dt / info[0]["iterations"],
            "residual": info[0]["residual"], "status": info[0]["status"],
            "path": "fused single-launch restart cycle"}
+    # the same solve preconditioned by the nested-dissection factorisation
+    # (factorisation inside the timed region)
+    def direct():
+        dp = P.DirectPrecond(plan, eps)
+        return P.solve(plan, eps, b, precond="direct", direct=dp, **kw)[1]
+    direct()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        infod = direct()
+    torch.cuda.synchronize()
+    dtd = (time.perf_counter() - t0) / n
+    out["direct"] = {"solves_per_s": 1.0 / dtd, "iterations": infod[0]["iterations"],
+                     "residual": infod[0]["residual"],
+                     "path": "FGMRES(30) + complex64 nested-dissection factors (factorisation timed)"}
     # 16 frequencies (lambda 1.50-1.60 um) solved as one batch
     lams = np.linspace(1.50e-6, 1.60e-6, 16)
     oms = 2 * np.pi * 299792458.0 / lams
@@ -233,6 +248,114 @@ def fdfd_numbers():
     t_lu = time.perf_counter() - t0
     out["cpu_spsolve"] = {"solves_per_s": 1.0 / t_lu, "cores": 1, "kind": "port",
                           "sample": "one 200x200 Ez solve, scipy SuperLU of the assembled matrix"}
+    return out
+
+
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def _solve_record(info, wall, n):
+    its = sorted(i["iterations"] for i in info)
+    conv = int(sum(i["code"] == 0 and i["residual"] <= 1e-6 for i in info))
+    return {"wall_s": wall, "problems": n, "converged_1e-6": conv,
+            "solves_per_s_at_1e-6": conv / wall,
+            "median_iterations": float(np.median(its)), "max_iterations": int(its[-1]),
+            "worst_residual": float(max(i["residual"] for i in info))}
+
+
+def fdfd_1e6_numbers(plain_cap4=2000, plain_cap5=300):
+    """The metric's FDFD half: solves/s at 1e-6 FP64 true residual through
+    the public primitives, inputs resident on the device.
+      config 4: 256 problems of 256x256 (binary eps, lambda 1.3-1.8 um) in one
+        batch; config 5: 2048x2048 with 16 omegas in one batch, Ez and Hz.
+    direct: flexible GMRES(30) preconditioned by the complex64
+    nested-dissection factorisation; the wall time counts the factorisation
+    (every problem has its own eps or omega) and the solve.  plain: restarted
+    GMRES(30) capped at `plain_cap` iterations (it does not reach 1e-6 on
+    these configurations); its residual is reported.  cpu_spsolve: the
+    reference's method (assembly + SuperLU) for one config-4 problem on one
+    host core."""
+    import torch
+    from ceviche_gb300 import primitives as P
+    from ceviche_gb300.workloads import config4_problem, config5
+    from oracle import fdfd as ofd
+    out = {}
+    probs = [config4_problem(i) for i in range(256)]
+    oms = np.array([q["omega"] for q in probs])
+    eps4 = torch.as_tensor(np.stack([q["eps"] for q in probs]), device="cuda")
+    b4 = torch.as_tensor(np.stack([1j * q["omega"] * q["src"] for q in probs]), device="cuda")
+    c4 = {}
+    for pol in ("ez", "hz"):
+        plan = P.Plan(pol, (256, 256), probs[0]["dL"], oms, probs[0]["npml"])
+
+        def direct():
+            dp = P.DirectPrecond(plan, eps4)
+            return P.solve(plan, eps4, b4, precond="direct", direct=dp, tol=1e-6)[1]
+        direct()  # grid analysis (cached per grid) and first-call costs
+        info, wall = _timed(direct)
+        rec = {"direct": _solve_record(info, wall, 256)}
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            info, wall = _timed(lambda: P.solve(plan, eps4, b4, tol=1e-6, max_iters=plain_cap4,
+                                                max_stall=10 ** 6)[1])
+        rec["plain"] = dict(_solve_record(info, wall, 256), iteration_cap=plain_cap4,
+                            median_residual=float(np.median([i["residual"] for i in info])))
+        c4[pol] = rec
+        del plan
+    q = probs[0]
+    A = ofd.make_A_ez(q["omega"], q["dL"], q["eps"], q["npml"])
+    t0 = time.perf_counter()
+    ofd.spsolve(A, 1j * q["omega"] * q["src"].ravel())
+    t_lu = time.perf_counter() - t0
+    c4["cpu_spsolve"] = {"solves_per_s": 1 / t_lu, "cores": 1, "kind": "port",
+                         "sample": "one 256x256 Ez problem, scipy SuperLU of the assembled matrix"}
+    out["config4_256x256_batch256"] = c4
+    del eps4, b4
+    torch.cuda.empty_cache()
+    q5 = config5()
+    n5 = q5["eps"].shape[0]
+    e5 = torch.as_tensor(q5["eps"], device="cuda")
+    b5 = torch.as_tensor(np.stack([1j * w * q5["src"] for w in q5["omegas"]]), device="cuda")
+    c5 = {}
+    for pol in ("ez", "hz"):
+        plan = P.Plan(pol, (n5, n5), q5["dL"], q5["omegas"], q5["npml"])
+        holder = {}
+
+        def direct():
+            holder["dp"] = P.DirectPrecond(plan, e5)
+            return P.solve(plan, e5, b5, precond="direct", direct=holder["dp"], tol=1e-6)[1]
+        direct()  # grid analysis (cached) and first-call costs
+        holder.clear()
+        torch.cuda.empty_cache()
+        info, wall = _timed(direct)
+        dp = holder.pop("dp")
+        _, t_fac = _timed(lambda: P.DirectPrecond(plan, e5))
+        r = torch.randn(16, n5, n5, dtype=torch.complex64, device="cuda")
+        _, t_app = _timed(lambda: dp.apply(r))
+        rec = {"direct": dict(_solve_record(info, wall, 16), factor_s=t_fac,
+                              factor_GB=dp.factor_bytes / 1e9,
+                              factor_TFMAs=4 * dp.factor_cmacs / t_fac / 1e12,
+                              apply_ms=1e3 * t_app, apply_GBps=dp.factor_bytes / t_app / 1e9)}
+        del dp, holder
+        torch.cuda.empty_cache()
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            info, wall = _timed(lambda: P.solve(plan, e5, b5, tol=1e-6, max_iters=plain_cap5,
+                                                max_stall=10 ** 6)[1])
+        rec["plain"] = dict(_solve_record(info, wall, 16), iteration_cap=plain_cap5,
+                            median_residual=float(np.median([i["residual"] for i in info])))
+        c5[pol] = rec
+        del plan
+        torch.cuda.empty_cache()
+    c5["cpu_spsolve"] = {"note": "not timed here: one 1024x1024 SuperLU solve took 63 s on one "
+                                 "core of the build machine; 2048x2048 is several hundred s"}
+    out["config5_2048x2048_16omega"] = c5
     return out
 
 
@@ -367,6 +490,10 @@ def run_ours(args):
                 line["fdfd"] = fdfd_numbers()
             except Exception as e:  # reported, never hidden
                 line["fdfd"] = {"error": repr(e)}
+            try:
+                line["fdfd_1e6"] = fdfd_1e6_numbers()
+            except Exception as e:
+                line["fdfd_1e6"] = {"error": repr(e)}
             try:
                 line["fdtd_scaled"] = fdtd_scaled_numbers()
             except Exception as e:
