@@ -304,12 +304,20 @@ struct TBArgs {
 
 // Most tiles one persistent tile exchanges its ring with.
 constexpr int NBR_MAX = 16;
+// Tile flags sit one 128-byte line apart (no two tiles' flags share a line).
+constexpr int FLAG_STRIDE = 32;
 
 __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
   int v;
   asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ void st_release_gpu(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -617,22 +625,20 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
       R* const* xb = a.xb[blk & 1];
       publish(xb);
       __syncthreads();
-      if (tid == 0) {
-        __threadfence();
-        st_release_gpu(a.flags + tile, blk + 1);
-      }
-      // bounded wait for the neighbours' block: about a second at most
+      // bar.sync orders the CTA's stores before thread 0's release
+      if (tid == 0) st_release_gpu(a.flags + tile * FLAG_STRIDE, blk + 1);
+      // bounded busy wait for the neighbours' block (about 2^24 L2 round
+      // trips at most, well under a minute)
       bool late = false;
       if (tid < NBR_MAX) {
         const int nb = a.nbr[tile * NBR_MAX + tid];
         if (nb >= 0) {
           int spins = 0;
-          while (ld_acquire_gpu(a.flags + nb) < blk + 1) {
-            if (++spins > (1 << 22) || ld_acquire_gpu(a.fault) != 0) {
+          while (ld_acquire_gpu(a.flags + nb * FLAG_STRIDE) < blk + 1) {
+            if (++spins > (1 << 24) || ((spins & 1023) == 0 && ld_acquire_gpu(a.fault) != 0)) {
               late = true;
               break;
             }
-            __nanosleep(128);
           }
         }
       }
@@ -676,6 +682,328 @@ __global__ void __launch_bounds__(NT, 1) k_tm_tile(TBArgs<R> a) {
   } else {
     R* const o[6] = {a.hx_o, a.hy_o, a.dz_o, a.icex_o, a.icey_o, a.idz_o};
     publish(o);
+  }
+}
+
+// ------------------------------------------------- register-strip TM kernel
+// The same K-step time-blocked recurrence as k_tm_tile with the state in
+// registers: lane l of warp w owns columns 2l and 2l+1 of rows w*S .. w*S+S-1
+// of a (W*S) x 64 region (interior (W*S - 2K) x (64 - 2K)).  Left and right
+// neighbours come by warp shuffle, up and down neighbours from the thread's
+// own rows; only the first Ez row and the last Hy row of each warp cross
+// shared memory, once per phase.  The PML form is evaluated for every cell of
+// a PML region (for a = 0 it reduces exactly to the interior form), and the
+// integrals are accumulated only where their coefficient is non-zero, as in
+// k_tm_tile.  PERSIST: the whole run in one cooperative launch with the ring
+// exchange of k_tm_tile.
+constexpr int STRIP_PROBE_MAX = 2048;
+
+template <int W, int S, int K>
+struct Strip {
+  static constexpr int RI = W * S, RJ = 64, TI = RI - 2 * K, TJ = RJ - 2 * K, NT = 32 * W;
+  static constexpr int RN = RI * RJ;
+  template <typename R>
+  static constexpr size_t smem(int np) {
+    return (size_t)RN * sizeof(R) + 2 * (size_t)W * RJ * sizeof(R) + 2 * (size_t)K * sizeof(R) +
+           (np > 0 ? (size_t)(RN + np) * sizeof(int) : 0);
+  }
+};
+
+template <typename R, int W, int S, int K, bool PERSIST>
+__global__ void __launch_bounds__(32 * W, 1) k_tm_strip(TBArgs<R> a) {
+  using G = Strip<W, S, K>;
+  constexpr int RI = G::RI, RJ = G::RJ, TI = G::TI, TJ = G::TJ, NT = G::NT, RN = G::RN;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R* sW = (R*)smraw;             // [RN] source weight per region cell
+  R* ezTop = sW + RN;            // [W][RJ] first Ez row of each warp
+  R* hyBot = ezTop + W * RJ;     // [W][RJ] last Hy row of each warp
+  R* sAmp = hyBot + W * RJ;      // [2][K]: this block's and the next block's amplitudes
+  int* sPid = (int*)(sAmp + 2 * K);  // [RN] first probe at a region cell (-1: none)
+  int* sPnext = sPid + RN;       // [np] next probe at the same cell
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int gi0 = blockIdx.y * TI - K, gj0 = blockIdx.x * TJ - K;
+  auto gi = [&](int r) { int v = (gi0 + r) % a.nx; return v < 0 ? v + a.nx : v; };
+  auto gj = [&](int c) { int v = (gj0 + c) % a.ny; return v < 0 ? v + a.ny : v; };
+  const int c0 = 2 * lane;
+  // coefficients: rows (x tables) and the thread's two columns (y tables)
+  R xf1[S], xf2[S], xg3[S], yf1[2], yf2[2], yg3[2];
+  R m1[S][2], m2[S][2], m4[S][2];
+  int pl = 0;
+  {
+    R xaD[S], xpD[S], yaD[2], ypD[2];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const AxisCoef<R> c = a.ax[gi(warp * S + s)];
+      xf1[s] = c.f1H; xf2[s] = c.f2H; xg3[s] = R(2) * c.aH; xaD[s] = c.aD; xpD[s] = c.pD;
+      pl |= (c.aH != R(0)) | (c.aD != R(0));
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const AxisCoef<R> c = a.ay[gj(c0 + q)];
+      yf1[q] = c.f1H; yf2[q] = c.f2H; yg3[q] = R(2) * c.aH; yaD[q] = c.aD; ypD[q] = c.pD;
+      pl |= (c.aH != R(0)) | (c.aD != R(0));
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const R ax = xaD[s], ay = yaD[q], pd = xpD[s] * ypD[q];
+        m1[s][q] = (R(1) - ax - ay - ax * ay) * pd;
+        m2[s][q] = a.S * pd;
+        m4[s][q] = R(-4) * ax * ay * pd;
+      }
+  }
+  for (int q = tid; q < RN; q += NT) sW[q] = R(0);
+  if (a.np > 0)
+    for (int q = tid; q < RN; q += NT) sPid[q] = -1;
+  const bool pml = __syncthreads_or(pl);
+  for (int k = tid; k < a.ns; k += NT) {
+    const int n = a.src_idx[k];
+    const int ii = n / a.ny, jj = n - ii * a.ny;
+    int r = (ii - gi0) % a.nx;
+    if (r < 0) r += a.nx;
+    int c = (jj - gj0) % a.ny;
+    if (c < 0) c += a.ny;
+    if (r < RI && c < RJ) atomicAdd(&sW[r * RJ + c], a.src_w[k]);
+  }
+  for (int k = tid; k < a.np; k += NT) {
+    const int n = a.probe_idx[k];
+    const int ii = n / a.ny, jj = n - ii * a.ny;
+    const int r = ii - gi0, c = jj - gj0;
+    if (r >= K && r < K + TI && c >= K && c < K + TJ) sPnext[k] = atomicExch(&sPid[r * RJ + c], k);
+  }
+  R hx[S][2], hy[S][2], dz[S][2], ie[S][2], ez[S][2], ix[S][2], iy[S][2], id[S][2];
+  // flat grid index of each owned cell (wrapped), and which of them this
+  // tile owns (interior, inside the grid) and publishes
+  int gofs[S][2];
+  unsigned srcmask = 0, probemask = 0, ownmask = 0, bandmask = 0;
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int r = warp * S + s, c = c0 + q;
+      gofs[s][q] = gi(r) * a.ny + gj(c);
+      if (r >= K && r < K + TI && c >= K && c < K + TJ && gi0 + r < a.nx && gj0 + c < a.ny) {
+        ownmask |= 1u << (2 * s + q);
+        // published at an exchange only if it lies in the ring of some
+        // neighbour (partial tiles at the grid edge wrap, so this is more
+        // than the K-wide band of the interior)
+        if (PERSIST) {
+          const int ii = gi0 + r, jj = gj0 + c;
+          const int gx = gridDim.x;
+          for (int k = 0; k < NBR_MAX; ++k) {
+            const int nb = a.nbr[(blockIdx.y * gx + blockIdx.x) * NBR_MAX + k];
+            if (nb < 0) break;
+            const int by = nb / gx, bx = nb - (nb / gx) * gx;
+            int dr = (ii - (by * TI - K)) % a.nx, dc = (jj - (bx * TJ - K)) % a.ny;
+            if (dr < 0) dr += a.nx;
+            if (dc < 0) dc += a.ny;
+            if (dr < RI && dc < RJ && !(dr >= K && dr < K + TI && dc >= K && dc < K + TJ))
+              bandmask |= 1u << (2 * s + q);
+          }
+        }
+      }
+      const size_t n = (size_t)gofs[s][q];
+      hx[s][q] = a.hx_i[n];
+      hy[s][q] = a.hy_i[n];
+      dz[s][q] = a.dz_i[n];
+      ie[s][q] = a.iez[n];
+      ix[s][q] = pml ? a.icex_i[n] : R(0);
+      iy[s][q] = pml ? a.icey_i[n] : R(0);
+      id[s][q] = pml ? a.idz_i[n] : R(0);
+      ez[s][q] = dz[s][q] * ie[s][q];
+      if (sW[r * RJ + c] != R(0)) srcmask |= 1u << (2 * s + q);
+      if (a.np > 0 && sPid[r * RJ + c] >= 0) probemask |= 1u << (2 * s + q);
+    }
+  const R Sc = a.S;
+  // warps without any PML coefficient take the interior form (for a = 0 the
+  // PML form gives the same numbers)
+  bool cell_pml = false;
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+#pragma unroll
+    for (int q = 0; q < 2; ++q)
+      cell_pml |= (xg3[s] != R(0)) | (yg3[q] != R(0)) | (m4[s][q] != R(0)) |
+                  (m1[s][q] != R(1)) | (m2[s][q] != Sc) | (xf1[s] != R(1)) | (yf1[q] != R(1)) |
+                  (xf2[s] != Sc) | (yf2[q] != Sc);
+  const bool wpml = pml && __any_sync(0xffffffffu, cell_pml);
+  const int wn = warp + 1 < W ? warp + 1 : warp;  // warp below (the last warp reads its own row)
+  const int wp = warp > 0 ? warp - 1 : warp;      // warp above
+  auto publish = [&](R* const* o, unsigned mask) {
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        if (mask & (1u << (2 * s + q))) {
+          const size_t n = (size_t)gofs[s][q];
+          o[0][n] = hx[s][q];
+          o[1][n] = hy[s][q];
+          o[2][n] = dz[s][q];
+          if (pml) {
+            o[3][n] = ix[s][q];
+            o[4][n] = iy[s][q];
+            o[5][n] = id[s][q];
+          }
+        }
+      }
+  };
+  ezTop[warp * RJ + c0] = ez[0][0];
+  ezTop[warp * RJ + c0 + 1] = ez[0][1];
+  __syncthreads();
+  const int nblk = PERSIST ? (a.nsteps + K - 1) / K : 1;
+  const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+  // amplitudes of a block's steps; the next block's are fetched before the
+  // neighbour wait, so no load latency sits between two blocks
+  auto load_amps = [&](int blk_) {
+    const int t0_ = PERSIST ? blk_ * K : a.t0;
+    const int n_ = PERSIST ? min(K, a.nsteps - t0_) : a.K;
+    for (int st = tid; st < n_; st += NT) sAmp[(blk_ & 1) * K + st] = a.ns > 0 ? a.amps[t0_ + st] : R(0);
+  };
+  load_amps(0);
+  __syncthreads();
+  for (int blk = 0; blk < nblk; ++blk) {
+    const int t0 = PERSIST ? blk * K : a.t0;
+    const int bst = PERSIST ? min(K, a.nsteps - t0) : a.K;
+    const R* amps = sAmp + (blk & 1) * K;
+    for (int st = 0; st < bst; ++st) {
+      // ---- H phase: Ez at (i, j+1) by shuffle, at (i+1, j) from the next row
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const R ezr = __shfl_down_sync(0xffffffffu, ez[s][0], 1);  // lane 31: its own (region edge)
+        const R right[2] = {ez[s][1], ezr};
+        R below[2];
+        if (s + 1 < S) {
+          below[0] = ez[s + 1][0];
+          below[1] = ez[s + 1][1];
+        } else {
+          below[0] = ezTop[wn * RJ + c0];
+          below[1] = ezTop[wn * RJ + c0 + 1];
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const R dEy = right[q] - ez[s][q];
+          const R dEx = -(below[q] - ez[s][q]);
+          if (!wpml) {
+            hx[s][q] = hx[s][q] - Sc * dEy;
+            hy[s][q] = hy[s][q] - Sc * dEx;
+          } else {
+            const R gx = xg3[s], gy = yg3[q];
+            R vx = R(0), vy = R(0);
+            if (gx != R(0)) { ix[s][q] += dEy; vx = ix[s][q]; }
+            if (gy != R(0)) { iy[s][q] += dEx; vy = iy[s][q]; }
+            hx[s][q] = yf1[q] * hx[s][q] - yf2[q] * (dEy + gx * vx);
+            hy[s][q] = xf1[s] * hy[s][q] - xf2[s] * (dEx + gy * vy);
+          }
+        }
+      }
+      hyBot[warp * RJ + c0] = hy[S - 1][0];
+      hyBot[warp * RJ + c0 + 1] = hy[S - 1][1];
+      __syncthreads();
+      // ---- D phase: Hx at (i, j-1) by shuffle, Hy at (i-1, j) from the row above
+      const R amp = amps[st];
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const R hxl0 = __shfl_up_sync(0xffffffffu, hx[s][1], 1);  // lane 0: its own (region edge)
+        const R left[2] = {hxl0, hx[s][0]};
+        R up[2];
+        if (s > 0) {
+          up[0] = hy[s - 1][0];
+          up[1] = hy[s - 1][1];
+        } else {
+          up[0] = hyBot[wp * RJ + c0];
+          up[1] = hyBot[wp * RJ + c0 + 1];
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const R ch = (hy[s][q] - up[q]) - (hx[s][q] - left[q]);
+          R v;
+          if (!wpml) {
+            v = dz[s][q] + Sc * ch;
+          } else {
+            R vd = R(0);
+            if (m4[s][q] != R(0)) {
+              id[s][q] += dz[s][q];
+              vd = id[s][q];
+            }
+            v = m1[s][q] * dz[s][q] + m2[s][q] * ch + m4[s][q] * vd;
+          }
+          if (srcmask & (1u << (2 * s + q))) v += sW[(warp * S + s) * RJ + c0 + q] * amp;
+          dz[s][q] = v;
+          ez[s][q] = v * ie[s][q];
+        }
+      }
+      ezTop[warp * RJ + c0] = ez[0][0];
+      ezTop[warp * RJ + c0 + 1] = ez[0][1];
+      if (probemask) {
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+          for (int q = 0; q < 2; ++q)
+            if (probemask & (1u << (2 * s + q)))
+              for (int k = sPid[(warp * S + s) * RJ + c0 + q]; k >= 0; k = sPnext[k])
+                a.probe_out[(size_t)(t0 + st) * a.np + k] = ez[s][q];
+      }
+      __syncthreads();
+    }
+    if constexpr (PERSIST) {
+      if (blk + 1 < nblk) {
+        R* const* xb = a.xb[blk & 1];
+        publish(xb, bandmask);
+        load_amps(blk + 1);
+        __syncthreads();
+        // bar.sync orders the CTA's stores before thread 0's release
+        if (tid == 0) st_release_gpu(a.flags + tile * FLAG_STRIDE, blk + 1);
+        bool late = false;
+        if (tid < NBR_MAX) {
+          const int nb = a.nbr[tile * NBR_MAX + tid];
+          if (nb >= 0) {
+            int spins = 0;
+            // busy poll (a sleep's granularity costs more than the wait);
+            // bounded: about 2^24 L2 round trips, well under a minute
+            // relaxed polls, one acquire fence once the flag is seen
+            while (ld_relaxed_gpu(a.flags + nb * FLAG_STRIDE) < blk + 1) {
+              if (++spins > (1 << 24) || ((spins & 1023) == 0 && ld_relaxed_gpu(a.fault) != 0)) {
+                late = true;
+                break;
+              }
+            }
+            fence_acq_rel_gpu();
+          }
+        }
+        if (__syncthreads_or(late)) {
+          if (tid == 0) atomicExch(a.fault, 1);
+          return;
+        }
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const int r = warp * S + s, c = c0 + q;
+            if (!(r >= K && r < K + TI && c >= K && c < K + TJ)) {
+              const size_t n = (size_t)gofs[s][q];
+              hx[s][q] = __ldcg(xb[0] + n);
+              hy[s][q] = __ldcg(xb[1] + n);
+              dz[s][q] = __ldcg(xb[2] + n);
+              if (pml) {
+                ix[s][q] = __ldcg(xb[3] + n);
+                iy[s][q] = __ldcg(xb[4] + n);
+                id[s][q] = __ldcg(xb[5] + n);
+              }
+              ez[s][q] = dz[s][q] * ie[s][q];
+            }
+          }
+        ezTop[warp * RJ + c0] = ez[0][0];
+        ezTop[warp * RJ + c0 + 1] = ez[0][1];
+        __syncthreads();
+      }
+    }
+  }
+  if constexpr (PERSIST) {
+    publish(a.xb[(nblk - 1) & 1], ownmask);
+  } else {
+    R* const o[6] = {a.hx_o, a.hy_o, a.dz_o, a.icex_o, a.icey_o, a.idz_o};
+    publish(o, ownmask);
   }
 }
 
@@ -1059,6 +1387,99 @@ static int pick_persist(int nx, int ny) {
   return -1;
 }
 
+// Register-strip configurations (warps, rows per thread, K); float32 only.
+struct StripCfg {
+  int w, s, k;
+};
+constexpr StripCfg STRIP_CFGS[] = {{16, 3, 8}, {16, 2, 4}, {16, 3, 4}, {32, 2, 8}};
+constexpr int N_STRIP_CFGS = sizeof(STRIP_CFGS) / sizeof(STRIP_CFGS[0]);
+
+static TileCfg strip_tile(const StripCfg& c) {
+  return TileCfg{c.w * c.s - 2 * c.k, 64 - 2 * c.k, c.k, 32 * c.w};
+}
+
+template <int I, bool P>
+struct StripLauncher {
+  static constexpr StripCfg c = STRIP_CFGS[I];
+  using G = Strip<c.w, c.s, c.k>;
+  static const void* fn() { return (const void*)k_tm_strip<float, c.w, c.s, c.k, P>; }
+  static int capacity(int np) {
+    const size_t smem = G::template smem<float>(np);
+    if (smem > 227 * 1024 || allow_dynamic_smem(fn(), (int)smem) != CEV_OK) {
+      cudaGetLastError();
+      return 0;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_tm_strip<float, c.w, c.s, c.k, P>, G::NT,
+                                                      smem) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    return n * sm_count();
+  }
+  static int launch(dim3 g, TBArgs<float>& a, int np, cudaStream_t s) {
+    const size_t smem = G::template smem<float>(np);
+    int rc = allow_dynamic_smem(fn(), (int)smem);
+    if (rc != CEV_OK) return rc;
+    if (P) {
+      void* args[] = {&a};
+      CEV_CUDA(cudaLaunchCooperativeKernel(fn(), g, dim3(G::NT), args, smem, s));
+    } else {
+      k_tm_strip<float, c.w, c.s, c.k, P><<<g, G::NT, smem, s>>>(a);
+      CEV_CHECK_LAUNCH("k_tm_strip");
+    }
+    return CEV_OK;
+  }
+};
+
+template <int I = 0>
+static int strip_capacity(int cfg, int np) {
+  if constexpr (I < N_STRIP_CFGS) {
+    return cfg == I ? StripLauncher<I, true>::capacity(np) : strip_capacity<I + 1>(cfg, np);
+  } else {
+    return 0;
+  }
+}
+
+template <int I = 0>
+static int strip_launch(int cfg, bool persist, dim3 g, TBArgs<float>& a, int np, cudaStream_t s) {
+  if constexpr (I < N_STRIP_CFGS) {
+    if (cfg == I)
+      return persist ? StripLauncher<I, true>::launch(g, a, np, s)
+                     : StripLauncher<I, false>::launch(g, a, np, s);
+    return strip_launch<I + 1>(cfg, persist, g, a, np, s);
+  } else {
+    set_error("bad strip configuration %d", cfg);
+    return CEV_ERR_INVALID;
+  }
+}
+
+// Register-strip configuration of the single-launch runner for this grid, or
+// -1.  CEV_FDTD_STRIP=0 turns it off, CEV_FDTD_STRIP=<i+1> forces
+// configuration i; a forced tile (CEV_FDTD_TILE) or persistent-tile
+// (CEV_FDTD_PERSIST) choice also turns it off.
+template <typename R>
+static int pick_strip(int nx, int ny, int np) {
+  if (sizeof(R) != sizeof(float)) return -1;
+  const char* e = std::getenv("CEV_FDTD_STRIP");
+  int forced = -1;
+  if (!e && (std::getenv("CEV_FDTD_TILE") || std::getenv("CEV_FDTD_PERSIST"))) return -1;
+  if (e) {
+    if (e[0] == '0') return -1;
+    forced = std::atoi(e) - 1;
+  }
+  if (np > STRIP_PROBE_MAX) return -1;
+  for (int v = 0; v < N_STRIP_CFGS; ++v) {
+    if (forced >= 0 && v != forced) continue;
+    if (forced < 0 && v != 0) continue;  // (16, 3, 8) by default
+    const TileCfg c = strip_tile(STRIP_CFGS[v]);
+    if (nx < c.ti + 2 * c.k || ny < c.tj + 2 * c.k) continue;
+    const int tiles = ((nx + c.ti - 1) / c.ti) * ((ny + c.tj - 1) / c.tj);
+    if (tiles <= strip_capacity(v, np)) return v;
+  }
+  return -1;
+}
+
 template <typename R>
 int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev_fdtd_io* io,
                 cudaStream_t s, R* dz_hist = nullptr) {
@@ -1098,12 +1519,24 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
   CEV_CUDA(cudaMemcpyAsync(bufB[3], bufA[3], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   CEV_CUDA(cudaMemcpyAsync(bufB[4], bufA[4], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
   CEV_CUDA(cudaMemcpyAsync(bufB[5], bufA[5], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
-  // single launch for grids whose tiles all fit on the GPU at once
-  const int pc = (dz_hist || p->borrowed) ? -1 : pick_persist<R>(p->nx, p->ny);
-  if (pc >= 0 && nsteps > PERSIST_CFGS[pc].k) {
-    const TileCfg c = PERSIST_CFGS[pc];
+  // single launch for grids whose tiles all fit on the GPU at once: the
+  // register-strip kernel (float32), else the persistent tile kernel
+  int pc = -1, key = -1;
+  TileCfg c{};
+  if (!dz_hist && !p->borrowed) {
+    const int si = pick_strip<R>(p->nx, p->ny, np);
+    if (si >= 0) {
+      pc = si;
+      key = 100 + si;
+      c = strip_tile(STRIP_CFGS[si]);
+    } else if ((pc = pick_persist<R>(p->nx, p->ny)) >= 0) {
+      key = pc;
+      c = PERSIST_CFGS[pc];
+    }
+  }
+  if (pc >= 0 && nsteps > c.k) {
     const int gy = (p->nx + c.ti - 1) / c.ti, gx = (p->ny + c.tj - 1) / c.tj;
-    if (p->pcfg != pc) {
+    if (p->pcfg != key) {
       std::vector<int> nbr;
       if (persist_neighbours(p->nx, p->ny, c, nbr)) {
         cudaFree(p->pnbr);
@@ -1113,12 +1546,12 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
         p->pcfg = -1;
         CEV_CUDA(cudaMalloc(&p->pnbr, sizeof(int) * nbr.size()));
         CEV_CUDA(cudaMemcpy(p->pnbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice));
-        CEV_CUDA(cudaMalloc(&p->pflags, sizeof(int) * (gx * gy + 1)));
-        p->pcfg = pc;
+        CEV_CUDA(cudaMalloc(&p->pflags, sizeof(int) * FLAG_STRIDE * (gx * gy + 1)));
+        p->pcfg = key;
         p->ptiles = gx * gy;
       }
     }
-    if (p->pcfg == pc) {
+    if (p->pcfg == key) {
       TBArgs<R> a{};
       a.nx = p->nx; a.ny = p->ny; a.K = c.k; a.t0 = 0;
       a.hx_i = bufA[0]; a.hy_i = bufA[1]; a.dz_i = bufA[2];
@@ -1140,10 +1573,18 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
         a.xb[1][f] = bufA[f];
       }
       a.flags = p->pflags;
-      a.fault = p->pflags + p->ptiles;
+      a.fault = p->pflags + (size_t)p->ptiles * FLAG_STRIDE;
       a.nbr = p->pnbr;
-      CEV_CUDA(cudaMemsetAsync(p->pflags, 0, sizeof(int) * (p->ptiles + 1), s));
-      int rc = persist_launch<R>(pc, dim3(gx, gy, 1), a, s);
+      CEV_CUDA(cudaMemsetAsync(p->pflags, 0, sizeof(int) * FLAG_STRIDE * (p->ptiles + 1), s));
+      int rc;
+      if (key >= 100) {
+        if constexpr (sizeof(R) == sizeof(float))
+          rc = strip_launch(pc, true, dim3(gx, gy, 1), a, np, s);
+        else
+          rc = CEV_ERR_INVALID;
+      } else {
+        rc = persist_launch<R>(pc, dim3(gx, gy, 1), a, s);
+      }
       if (rc != CEV_OK) return rc;
       const int nblk = (nsteps + c.k - 1) / c.k;
       if (((nblk - 1) & 1) == 0)  // the last block went to the shadow buffer

@@ -208,6 +208,41 @@ def test_every_persistent_configuration(cev, cfg, shape, steps, monkeypatch):
         assert _rel(_np(A.fields[k]), _np(B.fields[k])) < 1e-6
 
 
+@pytest.mark.parametrize("cfg", range(4))  # every entry of STRIP_CFGS in csrc/fdtd.cu
+@pytest.mark.parametrize("shape,steps", [((141, 133), 85), ((141, 133), 93), ((70, 70), 61)])
+def test_every_strip_configuration(cev, cfg, shape, steps, monkeypatch):
+    """The register-strip runner (forced through CEV_FDTD_STRIP; state in
+    registers, neighbours by warp shuffle, single launch with the ring
+    exchange) matches the per-step kernels: odd grids with PML, two sources
+    and four probes (two at the same cell), an odd and an even number of
+    K-step blocks, a 70x70 grid with a partial last tile row, and a second
+    run continuing from the first."""
+    monkeypatch.setenv("CEV_FDTD_STRIP", str(cfg + 1))
+    rng = np.random.default_rng(41)
+    Nx, Ny = shape
+    eps = 1 + 5 * rng.random((Nx, Ny))
+    dL, npml = 25e-9, [12, 9, 0]
+    src = np.zeros((Nx, Ny))
+    src[Nx // 2, 40] = 1.0
+    src[2, Ny - 2] = 0.3
+    amps = np.cos(0.3 * np.arange(steps)) * np.exp(-((np.arange(steps) - 15) / 8.0) ** 2)
+    probes = [(Nx // 2, 40), (0, 0), (Nx - 1, Ny - 1), (Nx // 2, 40)]
+    A = cev.fdtd(eps, dL, npml)
+    series = _np(A.run(steps, src, amps, probes))
+    series2 = _np(A.run(steps, src, amps, probes))
+    monkeypatch.setenv("CEV_FDTD_STRIP", "0")
+    monkeypatch.setenv("CEV_FDTD_PERSIST", "0")
+    B = cev.fdtd(eps, dL, npml)
+    ref = []
+    for rep in range(2):
+        for t in range(steps):
+            ez = _np(B.forward(Jz=src * amps[t])["Ez"])[:, :, 0]
+            ref.append([ez[i, j] for i, j in probes])
+    assert _rel(np.concatenate([series, series2]), np.array(ref)) < 1e-6
+    for k in ("Ez", "Hx", "Hy", "Dz"):
+        assert _rel(_np(A.fields[k]), _np(B.fields[k])) < 1e-6
+
+
 @pytest.mark.parametrize("precision,tol", [("float64", 1e-8), ("float32", 2e-4)])
 def test_per_step_autograd_like_reference_test(cev, precision, tol):
     """The reference gradient test pattern (test_gradients_fdtd.py:66-88):
