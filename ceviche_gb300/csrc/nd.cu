@@ -449,64 +449,94 @@ __global__ void __launch_bounds__(TILE) k_rowpanel(Args a, const int2* __restric
 }
 
 // Rank-nb update of every entry outside the pivot rows and columns:
-// F[r, c] -= F[r, p] R[p, c], one 64 x 64 tile per CTA (work: node, tile).
-// 128 threads, each an 8 x 4 block of the tile (rows ty + 8u, cols tx + 16v).
-__global__ void __launch_bounds__(128) k_update(Args a, const int2* __restrict__ work, int k0) {
-  __shared__ float2 Cp[TILE][NB + 1];
-  __shared__ float2 Rp[NB][TILE];
+// F[r, c] -= F[r, p] R[p, c], one UT_R x UT_C tile per CTA (work: node, tile).
+// 256 threads, each an 8 x 4 block (rows ty + 16u, cols tx + 16v).  Each
+// accumulator starts from the entry's old value, loaded before the panels,
+// so the read-modify-write latency overlaps the panel loads.
+constexpr int UT_R = 128, UT_C = 64;
+constexpr int UPD_SMEM = (UT_R * (NB + 1) + NB * UT_C) * (int)sizeof(float2);
+
+__global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restrict__ work, int k0) {
+  extern __shared__ float2 usm[];
+  float2(*Cp)[NB + 1] = (float2(*)[NB + 1])usm;                  // [UT_R][NB + 1]
+  float2(*Rp)[UT_C] = (float2(*)[UT_C])(usm + UT_R * (NB + 1));  // [NB][UT_C]
   const int2 w = work[blockIdx.x];
   const Node n = a.nodes[w.x];
   if (k0 >= n.nI) return;
   const int b = blockIdx.y;
-  const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
-  const int tiles = (f + TILE - 1) / TILE;
-  const int r0 = (w.y / tiles) * TILE, c0 = (w.y % tiles) * TILE;
-  // column panel F[r0 + i, k0 + k] (rows may be I or B rows; k0 + k < nI)
-  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
-    const int i = e / NB, k = e - i * NB;
-    const int r = r0 + i;
-    Cp[i][k] = (r < f && k < nb) ? *fel(a, n, b, r, k0 + k) : make_float2(0.f, 0.f);
-  }
-  const float2* rows = ftop(a, n, b);
-  for (int e = threadIdx.x; e < NB * TILE; e += blockDim.x) {
-    const int k = e / TILE, j = e - k * TILE;
-    const int c = c0 + j;
-    Rp[k][j] = (k < nb && c < f) ? rows[(size_t)(k0 + k) * f + c] : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
+  const int nI = n.nI, nB = n.nB;
+  const int nb = min(NB, nI - k0), f = nI + nB;
+  const int tc = (f + UT_C - 1) / UT_C;
+  const int r0 = (w.y / tc) * UT_R, c0 = (w.y % tc) * UT_C;
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  float2* const top = ftop(a, n, b);
+  float2* const bl = fbl(a, n, b);
+  float2* const sch = fsch(a, n, b);
+  // row r of the front: entries c < nI at lo[c], entries c >= nI at hi[c]
+  auto row_lo = [&](int r) { return r < nI ? top + (size_t)r * f : bl + (size_t)(r - nI) * nI; };
+  auto row_hi = [&](int r) {
+    return r < nI ? top + (size_t)r * f : sch + (size_t)(r - nI) * nB - nI;
+  };
+  // old values of this thread's entries (0 where outside or in the pivot block)
   float2 acc[8][4];
 #pragma unroll
-  for (int u = 0; u < 8; ++u)
+  for (int u = 0; u < 8; ++u) {
+    const int r = r0 + ty + 16 * u;
+    const bool rok = r < f && !(r >= k0 && r < k0 + nb);
+    const float2* lo = row_lo(min(r, f - 1));
+    const float2* hi = row_hi(min(r, f - 1));
 #pragma unroll
-    for (int v = 0; v < 4; ++v) acc[u][v] = make_float2(0.f, 0.f);
+    for (int v = 0; v < 4; ++v) {
+      const int c = c0 + tx + 16 * v;
+      acc[u][v] = (rok && c < f && !(c >= k0 && c < k0 + nb)) ? (c < nI ? lo[c] : hi[c])
+                                                               : make_float2(0.f, 0.f);
+    }
+  }
+  // column panel F[r0 + i, k0 + k] (rows may be I or B rows; k0 + k < nI)
+  {
+    const int k = threadIdx.x & (NB - 1);
+#pragma unroll 4
+    for (int i = threadIdx.x >> 5; i < UT_R; i += 8) {
+      const int r = r0 + i;
+      Cp[i][k] = (r < f && k < nb) ? row_lo(r)[k0 + k] : make_float2(0.f, 0.f);
+    }
+  }
+  {
+    const int j = threadIdx.x & (UT_C - 1);
+    const int c = c0 + j;
+#pragma unroll 4
+    for (int k = threadIdx.x >> 6; k < NB; k += 4)
+      Rp[k][j] = (k < nb && c < f) ? top[(size_t)(k0 + k) * f + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
 #pragma unroll 4
   for (int k = 0; k < NB; ++k) {
     float2 cv[8], rv[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) cv[u] = Cp[ty + 8 * u][k];
+    for (int u = 0; u < 8; ++u) cv[u] = Cp[ty + 16 * u][k];
 #pragma unroll
     for (int v = 0; v < 4; ++v) rv[v] = Rp[k][tx + 16 * v];
 #pragma unroll
     for (int u = 0; u < 8; ++u)
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        acc[u][v].x = fmaf(cv[u].x, rv[v].x, acc[u][v].x);
-        acc[u][v].x = fmaf(-cv[u].y, rv[v].y, acc[u][v].x);
-        acc[u][v].y = fmaf(cv[u].x, rv[v].y, acc[u][v].y);
-        acc[u][v].y = fmaf(cv[u].y, rv[v].x, acc[u][v].y);
+        acc[u][v].x = fmaf(-cv[u].x, rv[v].x, acc[u][v].x);
+        acc[u][v].x = fmaf(cv[u].y, rv[v].y, acc[u][v].x);
+        acc[u][v].y = fmaf(-cv[u].x, rv[v].y, acc[u][v].y);
+        acc[u][v].y = fmaf(-cv[u].y, rv[v].x, acc[u][v].y);
       }
   }
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
-    const int r = r0 + ty + 8 * u;
+    const int r = r0 + ty + 16 * u;
     if (r >= f || (r >= k0 && r < k0 + nb)) continue;
+    float2* lo = row_lo(r);
+    float2* hi = row_hi(r);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int c = c0 + tx + 16 * v;
       if (c >= f || (c >= k0 && c < k0 + nb)) continue;
-      float2* t = fel(a, n, b, r, c);
-      *t = csub(*t, acc[u][v]);
+      (c < nI ? lo : hi)[c] = acc[u][v];
     }
   }
 }
@@ -954,7 +984,8 @@ static int analyse(Shape& h, int nx, int ny, bool to_device) {
         if (n.child[s] >= 0)
           for (int r = 0; r < dn[n.child[s]].nB; ++r) L.ext[s].push_back(make_int2(k, r));
       for (int c = 0; c < nch; ++c) L.panel.push_back(make_int2(k, c));
-      for (int c = 0; c < nch * nch; ++c) L.tiles.push_back(make_int2(k, c));
+      const int ntiles = ((f + UT_R - 1) / UT_R) * ((f + UT_C - 1) / UT_C);
+      for (int c = 0; c < ntiles; ++c) L.tiles.push_back(make_int2(k, c));
       for (int c = 0; c < (n.nB + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.gemv.push_back(make_int2(k, c));
       for (int c = 0; c < (n.nI + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.bwd.push_back(make_int2(k, c));
     }
@@ -1081,6 +1112,10 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
     }
     if (L.large.empty()) continue;
     const unsigned nl = (unsigned)L.large.size();
+    {
+      const int rc = allow_dynamic_smem((const void*)k_update, UPD_SMEM);
+      if (rc != CEV_OK) return rc;
+    }
     k_orig<<<dim3(nl, B), 256, 0, s>>>(a, L.d_large);
     for (int sl = 0; sl < 2; ++sl)
       if (!L.ext[sl].empty())
@@ -1089,7 +1124,7 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
     for (int k0 = 0; k0 < L.max_nI_large; k0 += NB) {
       k_pivblock<<<dim3((nl + 3) / 4, B), 128, 0, s>>>(a, L.d_large, (int)nl, k0);
       k_rowpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
-      k_update<<<dim3((unsigned)L.tiles.size(), B), 128, 0, s>>>(a, L.d_tiles, k0);
+      k_update<<<dim3((unsigned)L.tiles.size(), B), 256, UPD_SMEM, s>>>(a, L.d_tiles, k0);
       k_colpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
     }
     CEV_CHECK_LAUNCH("nd sweep");
