@@ -470,7 +470,9 @@ CEV_API int cev_fdtd_run_tm(cev_fdtd_plan plan, const cev_fdtd_state* st, int ns
  * grids are rejected with CEV_ERR_INVALID.  The first call on a device looks
  * up the array's device address (cudaGetSymbolAddress); make that first call
  * before any stream capture.  Every call shares the array, so calls that
- * overlap on the GPU (other streams, other host threads) race.
+ * overlap on the GPU (other streams, other host threads) race.  A call
+ * enqueues kernels (its PML tables are computed on the device) and
+ * device-to-device copies only; it copies nothing from host memory.
  */
 CEV_API int cev_fdtd_run_tm_noalloc(int nx, int ny, double dL, int npml_x, int npml_y,
                                     const double* eps, const cev_fdtd_state* st, int nsteps,
