@@ -685,8 +685,9 @@ def config_numbers(max_iters5=1500):
     out["config3_adjoint_gradient_600x600"] = {
         "gpu_gradient_s": t_grad, "gpu_gradients_per_s": 1 / t_grad,
         "cpu_spsolve_forward_s": t_lu, "cpu_cores": 1,
-        "note": "GPU: forward + transposed plain GMRES(30) solves to 1e-6 and the gradient "
-                "kernel; CPU: one SuperLU forward solve (the adjoint needs a second)"}
+        "note": "GPU: forward + transposed FGMRES(30) solves to 1e-6 with the direct "
+                "preconditioner (the drop-in class default; factorisations timed) and the "
+                "gradient kernel; CPU: one SuperLU forward solve (the adjoint needs a second)"}
     # config 3b: FDTD reverse-time adjoint, 400x400, 4000 steps, checkpoints every 64
     from ceviche_gb300.workloads import config2
     p2 = config2(steps=4000)

@@ -113,16 +113,30 @@ class fdfd:
 
 class fdfd_ez(fdfd):
     """Ez polarisation: A = -(1/mu0)(Dxf Dxb + Dyf Dyb) - eps0 w^2 eps
-    (ceviche/fdfd.py:166-192).  solve(Jz) -> (Hx, Hy, Ez)."""
+    (ceviche/fdfd.py:166-192).  solve(Jz) -> (Hx, Hy, Ez).
+
+    Solves default to ``precond="direct"`` (complex64 nested-dissection
+    factors preconditioning flexible GMRES to the FP64 tolerance), the GPU
+    counterpart of the direct solve ceviche performs; ``precond="none"``
+    selects plain restarted GMRES."""
 
     pol = "ez"
+
+    def __init__(self, omega, dL, eps_r, npml, bloch_phases=None, **solver_opts):
+        solver_opts.setdefault("precond", "direct")
+        super().__init__(omega, dL, eps_r, npml, bloch_phases=bloch_phases, **solver_opts)
 
 
 class fdfd_hz(fdfd):
     """Hz polarisation: A = (1/eps0)(Dxb/eps_yy Dxf + Dyb/eps_xx Dyf) + mu0 w^2
-    (ceviche/fdfd.py:194-244).  solve(Mz) -> (Ex, Ey, Hz)."""
+    (ceviche/fdfd.py:194-244).  solve(Mz) -> (Ex, Ey, Hz).  Solves default to
+    ``precond="direct"`` as for fdfd_ez."""
 
     pol = "hz"
+
+    def __init__(self, omega, dL, eps_r, npml, bloch_phases=None, **solver_opts):
+        solver_opts.setdefault("precond", "direct")
+        super().__init__(omega, dL, eps_r, npml, bloch_phases=bloch_phases, **solver_opts)
 
 
 class fdfd_mf_ez(fdfd):
