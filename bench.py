@@ -362,6 +362,35 @@ def fdfd_1e6_numbers(plain_cap4=2000, plain_cap5=300):
     return out
 
 
+def fdtd_te_numbers(steps=2000):
+    """The TE polarisation (Hz, Dx, Dy with Jx, Jy point sources carrying the
+    config-2 pulse) on the config-2 grid through the time-blocked TE runner,
+    beside the TM headline."""
+    import torch
+    import ceviche_gb300 as cev
+    from ceviche_gb300.workloads import config2
+    p = config2()
+    F = cev.fdtd(p["eps"], p["dL"], p["npml"], precision="float32")
+    sx, sy = p["src"], -0.5 * p["src"]
+    F.run_te(steps, sx, sy, p["amps"])
+    stream = torch.cuda.current_stream()
+    ts = []
+    for _ in range(3):
+        F.initialize_fields()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        F.run_te(steps, sx, sy, p["amps"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+    t = min(ts)
+    cells = p["eps"].size * steps
+    return {"workload": "fdtd_te_400x400_2000steps (k_te_tile, 8 steps per launch)",
+            "value": cells / t / 1e9, "unit": UNIT,
+            "algorithmic_GBps": cells * 36 / t / 1e9,
+            "note": "36 B/cell-update algorithmic (Hz, Dx, Dy r+w, 1/eps_xx, 1/eps_yy r)"}
+
+
 def fdtd_scaled_numbers(steps=256):
     """Builder addition: the TM runner on a 4096x4096 grid (config-2 generator
     scaled by area), where the state (> 400 MB) does not fit in L2, so the
@@ -499,6 +528,10 @@ def run_ours(args):
                 line["fdfd_1e6"] = fdfd_1e6_numbers()
             except Exception as e:
                 line["fdfd_1e6"] = {"error": repr(e)}
+            try:
+                line["fdtd_te"] = fdtd_te_numbers()
+            except Exception as e:
+                line["fdtd_te"] = {"error": repr(e)}
             try:
                 line["fdtd_scaled"] = fdtd_scaled_numbers()
             except Exception as e:

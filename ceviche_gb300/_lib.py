@@ -42,6 +42,12 @@ class FDTDState(C.Structure):
                 ("hx", "hy", "dz", "icex", "icey", "idz", "hz", "dx", "dy", "ihz", "ichx", "ichy")]
 
 
+class FDTDIOTE(C.Structure):
+    _fields_ = [("n_src", C.c_int), ("src_idx", C.c_void_p), ("src_wx", C.c_void_p),
+                ("src_wy", C.c_void_p), ("amps", C.c_void_p), ("n_probe", C.c_int),
+                ("probe_idx", C.c_void_p), ("probe_out", C.c_void_p)]
+
+
 class FDTDIO(C.Structure):
     _fields_ = [("n_src", C.c_int), ("src_idx", C.c_void_p), ("src_w", C.c_void_p),
                 ("amps", C.c_void_p), ("n_probe", C.c_int), ("probe_idx", C.c_void_p),
@@ -110,6 +116,7 @@ SIGNATURES = {
     "cev_fdtd_step": (I, [P, C.POINTER(FDTDState), P, P, P, I, P]),
     "cev_fdtd_e_fields": (I, [P, C.POINTER(FDTDState), P, P, P, P]),
     "cev_fdtd_run_tm": (I, [P, C.POINTER(FDTDState), I, C.POINTER(FDTDIO), P]),
+    "cev_fdtd_run_te": (I, [P, C.POINTER(FDTDState), I, C.POINTER(FDTDIOTE), P]),
     "cev_fdtd_run_tm_noalloc": (I, [I, I, D, I, I, P, C.POINTER(FDTDState), I, C.POINTER(FDTDIO),
                                     P]),
     "cev_fdtd_step_adjoint_tm": (I, [P, P, P, P, C.POINTER(FDTDState), P, P, P]),

@@ -1643,6 +1643,299 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
   return CEV_OK;
 }
 
+// ------------------------------------------------------ time-blocked TE
+// The TE recurrence of k_te_h / k_te_d (ceviche/fdtd.py:79-137 with
+// Nz = 1: Hz from the curl of (Ex, Ey), then Dx, Dy from the curl of Hz, with
+// the Jx, Jy sources added to Dx, Dy) advanced K steps per launch on a
+// (TI + 2K) x (TJ + 2K) region in shared memory, as k_tm_tile does for TM:
+// the H phase needs E at i+1, j+1 and the D phase H at i-1, j-1, so the
+// interior is exact after K steps.  Sources: Jx(t) = wx * amps[t],
+// Jy(t) = wy * amps[t] at sparse cells; probes record Hz after each step.
+template <typename R>
+struct TEBArgs {
+  int nx, ny, K, t0;
+  const R* hz_i; const R* dx_i; const R* dy_i; const R* ih_i; const R* icx_i; const R* icy_i;
+  R* hz_o; R* dx_o; R* dy_o; R* ih_o; R* icx_o; R* icy_o;
+  const R* iexx;
+  const R* ieyy;
+  const AxisCoef<R>* ax;
+  const AxisCoef<R>* ay;
+  R S;
+  int ns;
+  const int* src_idx;
+  const R* src_wx;
+  const R* src_wy;
+  const R* amps;
+  int np;
+  const int* probe_idx;
+  R* probe_out;  // [t][np]
+};
+
+template <typename R, int TI, int TJ, int K, int NT>
+struct TeTile {
+  static constexpr int RI = TI + 2 * K, RJ = TJ + 2 * K, RN = RI * RJ;
+  static constexpr int CPT = (RN + NT - 1) / NT;
+  // sEx, sEy, sHz, sWx, sWy [RN]; x tables aH, pH, aD, f1D, f2D [RI]; y the same [RJ]; amps [K]
+  static constexpr size_t smem =
+      5 * (size_t)RN * sizeof(R) + 5 * (size_t)(RI + RJ) * sizeof(R) + (size_t)K * sizeof(R);
+};
+
+template <typename R, int TI, int TJ, int K, int NT>
+__global__ void __launch_bounds__(NT, 1) k_te_tile(TEBArgs<R> a) {
+  using T = TeTile<R, TI, TJ, K, NT>;
+  constexpr int RI = T::RI, RJ = T::RJ, RN = T::RN, CPT = T::CPT;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R* sEx = (R*)smraw;
+  R* sEy = sEx + RN;
+  R* sHz = sEy + RN;
+  R* sWx = sHz + RN;
+  R* sWy = sWx + RN;
+  R* xaH = sWy + RN;
+  R* xpH = xaH + RI;
+  R* xaD = xpH + RI;
+  R* xf1 = xaD + RI;
+  R* xf2 = xf1 + RI;
+  R* yaH = xf2 + RI;
+  R* ypH = yaH + RJ;
+  R* yaD = ypH + RJ;
+  R* yf1 = yaD + RJ;
+  R* yf2 = yf1 + RJ;
+  R* sAmp = yf2 + RJ;
+  const int nst = a.K;
+  const int gi0 = blockIdx.y * TI - K, gj0 = blockIdx.x * TJ - K;
+  const int tid = threadIdx.x;
+  auto gi = [&](int r) { int v = (gi0 + r) % a.nx; return v < 0 ? v + a.nx : v; };
+  auto gj = [&](int c) { int v = (gj0 + c) % a.ny; return v < 0 ? v + a.ny : v; };
+  int pl = 0;
+  for (int r = tid; r < RI; r += NT) {
+    const AxisCoef<R> c = a.ax[gi(r)];
+    xaH[r] = c.aH; xpH[r] = c.pH; xaD[r] = c.aD; xf1[r] = c.f1D; xf2[r] = c.f2D;
+    pl |= (c.aH != R(0)) | (c.aD != R(0));
+  }
+  for (int q = tid; q < RJ; q += NT) {
+    const AxisCoef<R> c = a.ay[gj(q)];
+    yaH[q] = c.aH; ypH[q] = c.pH; yaD[q] = c.aD; yf1[q] = c.f1D; yf2[q] = c.f2D;
+    pl |= (c.aH != R(0)) | (c.aD != R(0));
+  }
+  for (int st = tid; st < nst; st += NT) sAmp[st] = a.ns > 0 ? a.amps[a.t0 + st] : R(0);
+  for (int q = tid; q < RN; q += NT) {
+    sWx[q] = R(0);
+    sWy[q] = R(0);
+  }
+  const bool pml = __syncthreads_or(pl);
+  for (int k = tid; k < a.ns; k += NT) {
+    const int n = a.src_idx[k];
+    const int ii = n / a.ny, jj = n - ii * a.ny;
+    int r = (ii - gi0) % a.nx;
+    if (r < 0) r += a.nx;
+    int c = (jj - gj0) % a.ny;
+    if (c < 0) c += a.ny;
+    if (r < RI && c < RJ) {
+      atomicAdd(&sWx[r * RJ + c], a.src_wx[k]);
+      atomicAdd(&sWy[r * RJ + c], a.src_wy[k]);
+    }
+  }
+  __syncthreads();
+  R hz[CPT], dx[CPT], dy[CPT], iex[CPT], iey[CPT], ih[CPT], icx[CPT], icy[CPT];
+  unsigned srcmask = 0;
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int q = tid + k * NT;
+    hz[k] = dx[k] = dy[k] = iex[k] = iey[k] = ih[k] = icx[k] = icy[k] = R(0);
+    if (q < RN) {
+      const int r = q / RJ, c = q - r * RJ;
+      const size_t n = (size_t)gi(r) * a.ny + gj(c);
+      hz[k] = a.hz_i[n];
+      dx[k] = a.dx_i[n];
+      dy[k] = a.dy_i[n];
+      iex[k] = a.iexx[n];
+      iey[k] = a.ieyy[n];
+      if (pml) {
+        ih[k] = a.ih_i[n];
+        icx[k] = a.icx_i[n];
+        icy[k] = a.icy_i[n];
+      }
+      if (sWx[q] != R(0) || sWy[q] != R(0)) srcmask |= 1u << k;
+      sEx[q] = dx[k] * iex[k];
+      sEy[q] = dy[k] * iey[k];
+    }
+  }
+  __syncthreads();
+  const R S = a.S;
+  for (int st = 0; st < nst; ++st) {
+    const R amp = sAmp[st];
+    // ---- H phase: Hz from the curl of (Ex, Ey)
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+      const int q = tid + k * NT;
+      if (q < RN) {
+        const int r = q / RJ, c = q - r * RJ;
+        const R ex = sEx[q], ey = sEy[q];
+        const R exr = (c < RJ - 1) ? sEx[q + 1] : ex;
+        const R eyd = (r < RI - 1) ? sEy[q + RJ] : ey;
+        const R ce = (eyd - ey) - (exr - ex);
+        if (!pml) {
+          hz[k] = hz[k] - S * ce;
+        } else {
+          const R ax = xaH[r], ay = yaH[c];
+          const R ph = xpH[r] * ypH[c];
+          const R m1 = (R(1) - ax - ay - ax * ay) * ph;
+          const R m2 = -S * ph;
+          const R m4 = R(-4) * ax * ay * ph;
+          R v = R(0);
+          if (m4 != R(0)) { ih[k] += hz[k]; v = ih[k]; }
+          hz[k] = m1 * hz[k] + m2 * ce + m4 * v;
+        }
+        sHz[q] = hz[k];
+      }
+    }
+    __syncthreads();
+    // ---- D phase: Dx, Dy from the curl of Hz, plus the sources
+#pragma unroll
+    for (int k = 0; k < CPT; ++k) {
+      const int q = tid + k * NT;
+      if (q < RN) {
+        const int r = q / RJ, c = q - r * RJ;
+        const R hzl = (c > 0) ? sHz[q - 1] : hz[k];
+        const R hzu = (r > 0) ? sHz[q - RJ] : hz[k];
+        const R chx = hz[k] - hzl;
+        const R chy = -(hz[k] - hzu);
+        R vx, vy;
+        if (!pml) {
+          vx = dx[k] + S * chx;
+          vy = dy[k] + S * chy;
+        } else {
+          const R ax = xaD[r], ay = yaD[c];
+          R wx = R(0), wy = R(0);
+          if (ax != R(0)) { icx[k] += chx; wx = icx[k]; }
+          if (ay != R(0)) { icy[k] += chy; wy = icy[k]; }
+          vx = yf1[c] * dx[k] + yf2[c] * (chx + R(2) * ax * wx);
+          vy = xf1[r] * dy[k] + xf2[r] * (chy + R(2) * ay * wy);
+        }
+        if (srcmask & (1u << k)) {
+          vx += sWx[q] * amp;
+          vy += sWy[q] * amp;
+        }
+        dx[k] = vx;
+        dy[k] = vy;
+        sEx[q] = vx * iex[k];
+        sEy[q] = vy * iey[k];
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < a.np; k += NT) {
+      const int n = a.probe_idx[k];
+      const int ii = n / a.ny, jj = n - ii * a.ny;
+      const int r = ii - gi0, c = jj - gj0;
+      if (r >= K && r < K + TI && c >= K && c < K + TJ)
+        a.probe_out[(size_t)(a.t0 + st) * a.np + k] = sHz[r * RJ + c];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < CPT; ++k) {
+    const int q = tid + k * NT;
+    if (q < RN) {
+      const int r = q / RJ, c = q - r * RJ;
+      const int ii = gi0 + r, jj = gj0 + c;
+      if (r >= K && r < K + TI && c >= K && c < K + TJ && ii < a.nx && jj < a.ny) {
+        const size_t n = (size_t)ii * a.ny + jj;
+        a.hz_o[n] = hz[k];
+        a.dx_o[n] = dx[k];
+        a.dy_o[n] = dy[k];
+        if (pml) {
+          a.ih_o[n] = ih[k];
+          a.icx_o[n] = icx[k];
+          a.icy_o[n] = icy[k];
+        }
+      }
+    }
+  }
+}
+
+// per-step TE extras of the fallback: sparse Jx/Jy sources and Hz probes
+template <typename R>
+__global__ void k_add_src_te(R* dx, R* dy, int ns, const int* idx, const R* wx, const R* wy,
+                             const R* amps, int t) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  dx[idx[k]] += wx[k] * amps[t];
+  dy[idx[k]] += wy[k] * amps[t];
+}
+
+template <typename R>
+__global__ void k_probe_hz(const R* hz, int np, const int* idx, R* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < np) out[k] = hz[idx[k]];
+}
+
+// TE tile shape: 32 x 48 interior, K = 8, 512 threads (the TM choice at 400^2)
+constexpr int TE_TI = 32, TE_TJ = 48, TE_K = 8, TE_NT = 512;
+
+template <typename R>
+int run_te_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev_fdtd_io_te* io,
+                cudaStream_t s) {
+  const size_t N = p->n();
+  const int ns = io ? io->n_src : 0, np = io ? io->n_probe : 0;
+  if (p->nx < TE_TI + 2 * TE_K || p->ny < TE_TJ + 2 * TE_K) {
+    // grids smaller than one tile region: per-step kernels
+    for (int t = 0; t < nsteps; ++t) {
+      int rc = step_impl<R>(p, st, nullptr, nullptr, nullptr, 1, s);
+      if (rc != CEV_OK) return rc;
+      if (ns > 0)
+        k_add_src_te<R><<<(ns + 127) / 128, 128, 0, s>>>(
+            (R*)st->dx, (R*)st->dy, ns, io->src_idx, (const R*)io->src_wx, (const R*)io->src_wy,
+            (const R*)io->amps, t);
+      if (np > 0)
+        k_probe_hz<R><<<(np + 127) / 128, 128, 0, s>>>((const R*)st->hz, np, io->probe_idx,
+                                                        (R*)io->probe_out + (size_t)t * np);
+    }
+    CEV_CHECK_LAUNCH("fdtd run te (per step)");
+    return CEV_OK;
+  }
+  if (!p->shadow) {
+    CEV_REQUIRE(!p->borrowed, "borrowed FDTD plan without a shadow state");
+    CEV_CUDA(cudaMalloc(&p->shadow, 6 * N * sizeof(R)));
+  }
+  R* sh = (R*)p->shadow;
+  R* bufA[6] = {(R*)st->hz, (R*)st->dx, (R*)st->dy, (R*)st->ihz, (R*)st->ichx, (R*)st->ichy};
+  R* bufB[6] = {sh, sh + N, sh + 2 * N, sh + 3 * N, sh + 4 * N, sh + 5 * N};
+  // the shadow's PML integrals must match the state outside tiles that skip them
+  for (int f = 3; f < 6; ++f)
+    CEV_CUDA(cudaMemcpyAsync(bufB[f], bufA[f], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+  using T = TeTile<R, TE_TI, TE_TJ, TE_K, TE_NT>;
+  int rc = allow_dynamic_smem((const void*)k_te_tile<R, TE_TI, TE_TJ, TE_K, TE_NT>, (int)T::smem);
+  if (rc != CEV_OK) return rc;
+  const dim3 g((p->ny + TE_TJ - 1) / TE_TJ, (p->nx + TE_TI - 1) / TE_TI, 1);
+  R** in = bufA;
+  R** out = bufB;
+  TEBArgs<R> a{};
+  for (int t = 0; t < nsteps; t += TE_K) {
+    a.nx = p->nx; a.ny = p->ny; a.K = std::min(TE_K, nsteps - t); a.t0 = t;
+    a.hz_i = in[0]; a.dx_i = in[1]; a.dy_i = in[2]; a.ih_i = in[3]; a.icx_i = in[4]; a.icy_i = in[5];
+    a.hz_o = out[0]; a.dx_o = out[1]; a.dy_o = out[2]; a.ih_o = out[3]; a.icx_o = out[4]; a.icy_o = out[5];
+    a.iexx = (const R*)p->iexx;
+    a.ieyy = (const R*)p->ieyy;
+    a.ax = (const AxisCoef<R>*)p->ax;
+    a.ay = (const AxisCoef<R>*)p->ay;
+    a.S = (R)p->S;
+    a.ns = ns;
+    a.src_idx = ns ? io->src_idx : nullptr;
+    a.src_wx = ns ? (const R*)io->src_wx : nullptr;
+    a.src_wy = ns ? (const R*)io->src_wy : nullptr;
+    a.amps = ns ? (const R*)io->amps : nullptr;
+    a.np = np;
+    a.probe_idx = np ? io->probe_idx : nullptr;
+    a.probe_out = np ? (R*)io->probe_out : nullptr;
+    k_te_tile<R, TE_TI, TE_TJ, TE_K, TE_NT><<<g, TE_NT, T::smem, s>>>(a);
+    CEV_CHECK_LAUNCH("k_te_tile");
+    std::swap(in, out);
+  }
+  if (in != bufA)
+    for (int f = 0; f < 6; ++f)
+      CEV_CUDA(cudaMemcpyAsync(bufA[f], in[f], N * sizeof(R), cudaMemcpyDeviceToDevice, s));
+  return CEV_OK;
+}
+
 template <typename R>
 int adjoint_impl(cev_fdtd_plan p, int T, int C, const cev_fdtd_io* io, const R* w, double* geps,
                  void* ws, cudaStream_t s) {
@@ -1855,6 +2148,22 @@ int cev_fdtd_run_tm(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const
   if (nsteps == 0) return CEV_OK;
   if (p->prec == CEV_PREC_C128) return run_tm_impl<double>(p, st, nsteps, io, s);
   return run_tm_impl<float>(p, st, nsteps, io, s);
+}
+
+int cev_fdtd_run_te(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps,
+                    const cev_fdtd_io_te* io, cudaStream_t s) {
+  CEV_REQUIRE(p && st, "NULL argument");
+  CEV_REQUIRE(nsteps >= 0, "nsteps must be >= 0");
+  CEV_REQUIRE(st->hz && st->dx && st->dy && st->ihz && st->ichx && st->ichy, "TE state incomplete");
+  if (io) {
+    CEV_REQUIRE(io->n_src >= 0 && io->n_probe >= 0, "negative source/probe count");
+    CEV_REQUIRE(io->n_src == 0 || (io->src_idx && io->src_wx && io->src_wy && io->amps),
+                "source arrays missing");
+    CEV_REQUIRE(io->n_probe == 0 || (io->probe_idx && io->probe_out), "probe arrays missing");
+  }
+  if (nsteps == 0) return CEV_OK;
+  if (p->prec == CEV_PREC_C128) return run_te_impl<double>(p, st, nsteps, io, s);
+  return run_te_impl<float>(p, st, nsteps, io, s);
 }
 
 int cev_fdtd_step_adjoint_tm(cev_fdtd_plan p, const void* dz_in, const void* dz_out,

@@ -256,6 +256,59 @@ class fdtd:
         return out
 
 
+    def run_te(self, steps, source_x=None, source_y=None, amps=None, probes=None):
+        """Advance ``steps`` TE steps with Jx(t) = source_x * amps[t] and
+        Jy(t) = source_y * amps[t] (time-blocked, cev_fdtd_run_te); returns
+        the (steps, n_probe) series of Hz at ``probes`` (or None).  The TM
+        fields do not change (Nz = 1: the polarisations are independent)."""
+        lib = _lib.load()
+        if self._te is None:
+            self._te = {k: torch.zeros((self.Nx, self.Ny), dtype=self.dtype, device="cuda")
+                        for k in _TE}
+        keep = []
+        io = _lib.FDTDIOTE()
+        if source_x is not None or source_y is not None:
+            def prof(src):
+                if src is None:
+                    return torch.zeros(self.Nx * self.Ny, dtype=torch.float64)
+                t = src if torch.is_tensor(src) else torch.as_tensor(np.asarray(src))
+                return t.detach().to("cpu", torch.float64).reshape(-1)
+            px, py = prof(source_x), prof(source_y)
+            idx = torch.nonzero((px != 0) | (py != 0)).reshape(-1)
+            a = amps if torch.is_tensor(amps) else torch.as_tensor(np.asarray(amps))
+            a = a.detach().to("cuda", self.dtype).reshape(-1).contiguous()
+            if a.numel() < steps:
+                raise ValueError(f"amps has {a.numel()} entries, need {steps}")
+            idx_d = idx.to("cuda", torch.int32).contiguous()
+            wx = px[idx].to("cuda", self.dtype).contiguous()
+            wy = py[idx].to("cuda", self.dtype).contiguous()
+            keep += [idx_d, wx, wy, a]
+            io.n_src = int(idx.numel())
+            io.src_idx, io.src_wx, io.src_wy, io.amps = (idx_d.data_ptr(), wx.data_ptr(),
+                                                         wy.data_ptr(), a.data_ptr())
+        out = None
+        if probes is not None and len(probes) > 0:
+            pidx = torch.as_tensor([int(i) * self.Ny + int(j) for i, j in probes],
+                                   dtype=torch.int32, device="cuda")
+            out = torch.zeros((steps, len(probes)), dtype=self.dtype, device="cuda")
+            keep += [pidx, out]
+            io.n_probe = len(probes)
+            io.probe_idx, io.probe_out = pidx.data_ptr(), out.data_ptr()
+        st = self._state()
+        check(lib.cev_fdtd_run_te(self._plan_h, C.byref(st), int(steps), C.byref(io),
+                                  stream_ptr()), "fdtd_run_te")
+        self.t_index += steps
+        ex = torch.empty((self.Nx, self.Ny), dtype=self.dtype, device="cuda")
+        ey = torch.empty_like(ex)
+        check(lib.cev_fdtd_e_fields(self._plan_h, C.byref(st), ptr(ex), ptr(ey), None,
+                                    stream_ptr()), "fdtd_e_fields")
+        v3 = lambda t: t.view(self.Nx, self.Ny, 1)
+        self.fields.update(Hz=v3(self._te["hz"]), Dx=v3(self._te["dx"]), Dy=v3(self._te["dy"]),
+                           Ex=v3(ex), Ey=v3(ey))
+        del keep
+        return out
+
+
 class _TMStep(torch.autograd.Function):
     """One TM step, out of place: (eps, jz, state) -> (new state, Ez)."""
 

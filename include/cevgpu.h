@@ -457,6 +457,28 @@ typedef struct {
 CEV_API int cev_fdtd_run_tm(cev_fdtd_plan plan, const cev_fdtd_state* st, int nsteps,
                     const cev_fdtd_io* io, cudaStream_t stream);
 
+/* Sparse TE sources J(t) = (wx, wy) * amps[t] at cells idx_k, and Hz probes. */
+typedef struct {
+  int n_src;
+  const int* src_idx;   /* device, flat cell indices */
+  const void* src_wx;   /* device, field precision: Jx weight per source cell */
+  const void* src_wy;   /* device, field precision: Jy weight per source cell */
+  const void* amps;     /* device, field precision, amps[t - t_begin] */
+  int n_probe;
+  const int* probe_idx; /* device, flat cell indices */
+  void* probe_out;      /* device, field precision, [nsteps][n_probe] Hz after each step */
+} cev_fdtd_io_te;
+
+/*
+ * nsteps TE steps (Hz, Dx, Dy with Jx, Jy sources: the TE half of
+ * ceviche/fdtd.py:79-137 with Nz = 1), time-blocked like cev_fdtd_run_tm
+ * (K = 8 steps per launch on 32 x 48 tiles; per-step kernels on grids below
+ * one tile region).  Bitwise the same recurrence as cev_fdtd_step with te = 1
+ * and dense Jx = wx * amps[t], Jy = wy * amps[t].
+ */
+CEV_API int cev_fdtd_run_te(cev_fdtd_plan plan, const cev_fdtd_state* st, int nsteps,
+                            const cev_fdtd_io_te* io, cudaStream_t stream);
+
 /*
  * Allocation-free variant of cev_fdtd_run_tm.  No counterpart in the
  * reference.  For callers that cannot allocate device memory (a host

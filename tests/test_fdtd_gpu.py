@@ -243,6 +243,38 @@ def test_every_strip_configuration(cev, cfg, shape, steps, monkeypatch):
         assert _rel(_np(A.fields[k]), _np(B.fields[k])) < 1e-6
 
 
+@pytest.mark.parametrize("precision", ["float32", "float64"])
+@pytest.mark.parametrize("shape", [(96, 80), (131, 77), (40, 36)])
+def test_te_runner_matches_steps(cev, precision, shape):
+    """Time-blocked TE runner (cev_fdtd_run_te; per-step kernels below one
+    tile region, 40x36) == per-step TE kernels with dense Jx, Jy (sources in
+    the PML and near the periodic wrap, probes, two runs in a row)."""
+    rng = np.random.default_rng(17)
+    Nx, Ny = shape
+    eps = 1 + 5 * rng.random((Nx, Ny))
+    dL, npml, steps = 25e-9, [10, 7, 0], 45
+    sx = np.zeros((Nx, Ny))
+    sy = np.zeros((Nx, Ny))
+    sx[Nx // 2, Ny // 3] = 1.0
+    sy[Nx // 2, Ny // 3] = -0.4
+    sy[3, Ny - 2] = 0.7
+    amps = np.sin(0.2 * np.arange(steps)) * np.exp(-((np.arange(steps) - 20) / 10.0) ** 2)
+    probes = [(Nx // 2, Ny // 3), (0, 0), (Nx - 1, Ny - 1), (20, 21)]
+    A = cev.fdtd(eps, dL, npml, precision=precision)
+    series = np.concatenate([_np(A.run_te(steps, sx, sy, amps, probes)) for _ in range(2)])
+    B = cev.fdtd(eps, dL, npml, precision=precision)
+    ref = []
+    for rep in range(2):
+        for t in range(steps):
+            f = B.forward(Jx=sx * amps[t], Jy=sy * amps[t])
+            hz = _np(f["Hz"])[:, :, 0]
+            ref.append([hz[i, j] for i, j in probes])
+    tol = 1e-6 if precision == "float32" else 1e-13
+    assert _rel(series, np.array(ref)) < tol
+    for k in ("Hz", "Dx", "Dy", "Ex", "Ey"):
+        assert _rel(_np(A.fields[k]), _np(B.fields[k])) < tol, k
+
+
 @pytest.mark.parametrize("precision,tol", [("float64", 1e-8), ("float32", 2e-4)])
 def test_per_step_autograd_like_reference_test(cev, precision, tol):
     """The reference gradient test pattern (test_gradients_fdtd.py:66-88):
