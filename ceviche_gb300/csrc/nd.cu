@@ -32,8 +32,9 @@
 // alternating by depth parity (a node's children are one depth deeper).
 //
 // Kernels.  Fronts with f <= 128 (the lower levels, most nodes) are assembled
-// and swept entirely in shared memory, one CTA per (node, problem), each
-// thread holding its block of F in registers.  Larger fronts are assembled in
+// and swept entirely in shared memory, one CTA per (node, problem), in blocks
+// of up to 16 pivots (LU of the pivot block, triangular-solve panels, a
+// register-tiled rank-16 update).  Larger fronts are assembled in
 // global memory and swept in blocks of NB = 32 pivots: invert the pivot block,
 // scale the pivot rows, a rank-32 update of every other entry (64 x 64 tiles,
 // FP32 FMA), and scale the pivot columns; the rank-32 update carries the
@@ -209,27 +210,201 @@ __global__ void k_zero(float2* base, long long pp, long long lo, long long len, 
 }
 
 // ============================================================ small fronts
-// One CTA per (node, problem): assemble F (f <= FS) in shared memory, keep
-// each thread's TR x TC-strided block of it in registers through the
-// Gauss-Jordan sweep, write [G | H] and -K (column-major) and S out.
-template <int FS, int TR, int TC>
-__global__ void __launch_bounds__(TR * TC) k_small(Args a, const int* __restrict__ list) {
-  constexpr int R = FS / TR, Cn = FS / TC;
-  extern __shared__ float2 sm[];
-  float2* F = sm;                 // f x f, row stride f
-  float2* rowbuf = sm + FS * FS;  // FS
-  float2* colbuf = rowbuf + FS;   // FS
-  __shared__ float2 s_pinv;
+__device__ __forceinline__ float2 shfl2(float2 v, int src) {
+  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// Visits e = start, start + step, ... < total as (e, e / d, e % d) with one
+// division up front instead of one per element.
+template <typename Fn>
+__device__ __forceinline__ void for_divmod(int start, int step, int total, int d, Fn&& fn) {
+  int q = start / d, r = start - q * d;
+  const int sq = step / d, sr = step - sq * d;
+  for (int e = start; e < total; e += step) {
+    fn(e, q, r);
+    q += sq;
+    r += sr;
+    if (r >= d) {
+      r -= d;
+      ++q;
+    }
+  }
+}
+
+// Writes the swept front (row stride ld in shared memory) to the factor:
+// [G | H] and -K column-major, S row-major.
+__device__ __forceinline__ void store_small(const Args& a, const Node& n, int b, const float2* F,
+                                            int ld, int tid, int nt) {
+  const int nI = n.nI, nB = n.nB, f = nI + nB;
+  float2* top = ftop(a, n, b);
+  float2* bl = fbl(a, n, b);
+  float2* S = fsch(a, n, b);
+  for_divmod(tid, nt, nI * f, nI, [&](int e, int c, int r) { top[e] = F[r * ld + c]; });
+  if (nB == 0) return;
+  for_divmod(tid, nt, nB * nI, nB, [&](int e, int c, int r) { bl[e] = F[(nI + r) * ld + c]; });
+  for_divmod(tid, nt, nB * nB, nB, [&](int e, int r, int c) { S[e] = F[(nI + r) * ld + nI + c]; });
+}
+
+// Leaves (childless fronts, nI <= 16, nB <= 16): F_BB = 0 and every boundary
+// cell j couples to exactly one interior cell i_j, from one side (the frame of
+// a box without its corners), so with G = F_II^-1 the sweep operator is
+//   H[:, j] = G[:, i_j] a_j,   -K[j, :] = -b_j G[i_j, :],
+//   S[j, l] = -b_j G[i_j, i_l] a_l,      a_j = F[i_j, j], b_j = F[j, i_j]:
+// only the nI x nI inverse is computed.  One warp per (leaf, problem), no
+// CTA barrier; G is swept pivot by pivot in registers (lane 2r + h holds
+// columns 8h .. 8h + 7 of row r), the pivot row and column by shuffles, with
+// partial pivoting: swapping two rows not yet swept swaps two equations, so
+// the sweep yields (Pm F_II)^-1 = F_II^-1 Pm^T, whose columns are put back
+// in order when G is stored.
+constexpr int LEAF_WARPS = 4;
+__global__ void __launch_bounds__(LEAF_WARPS * 32) k_leaf(Args a, const int* __restrict__ list,
+                                                          int count) {
+  __shared__ float2 Gs[LEAF_WARPS][16][17];
+  __shared__ float2 av[LEAF_WARPS][16], bv[LEAF_WARPS][16];
+  __shared__ int ia[LEAF_WARPS][16], ib[LEAF_WARPS][16];
+  __shared__ int lperm[LEAF_WARPS][16];  // row i of the swept matrix is row lperm[i] of F_II
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int item = blockIdx.x * LEAF_WARPS + warp;
+  if (item >= count) return;  // warp-uniform; the kernel has no CTA barrier
+  const Node n = a.nodes[list[item]];
+  const int b = blockIdx.y;
+  const int nI = n.nI, nB = n.nB, f = nI + nB;
+  float2(*G)[17] = Gs[warp];
+  for (int e = lane; e < 256; e += 32) G[e >> 4][e & 15] = make_float2(0.f, 0.f);
+  if (lane < 16) lperm[warp][lane] = lane;
+  __syncwarp();
+  for (int q = lane; q < n.ndesc; q += 32) {
+    const Desc d = a.desc[n.desc + q];  // (row, col) pairs are distinct
+    const float2 v = coef(a.op, b, d.cell, d.dir);
+    if (d.row < nI) {
+      if (d.col < nI) {
+        G[d.row][d.col] = v;
+      } else {
+        av[warp][d.col - nI] = v;
+        ia[warp][d.col - nI] = d.row;
+      }
+    } else {
+      bv[warp][d.row - nI] = v;
+      ib[warp][d.row - nI] = d.col;
+    }
+  }
+  __syncwarp();
+  const int r = lane >> 1, h = lane & 1;
+  float2 x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = G[r][8 * h + k];
+  for (int p = 0; p < nI; ++p) {
+    // F[r, p] sits in lane 2r + p / 8, slot p % 8; F[p, 8h + k] in lane 2p + h, slot k
+    float2 mine = x[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k)
+      if ((p & 7) == k) mine = x[k];
+    float2 colv = shfl2(mine, 2 * r + (p >> 3));
+    // pivot row: the largest |F[q, p]| among rows p .. nI-1 (lowest row on ties)
+    float m = (h == 0 && r >= p && r < nI) ? colv.x * colv.x + colv.y * colv.y : -1.f;
+    int q = r;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float m2 = __shfl_xor_sync(0xffffffffu, m, o);
+      const int q2 = __shfl_xor_sync(0xffffffffu, q, o);
+      if (m2 > m || (m2 == m && q2 < q)) {
+        m = m2;
+        q = q2;
+      }
+    }
+    if (q != p) {  // warp-uniform: rows p and q trade places
+      const int src = r == p ? 2 * q + h : (r == q ? 2 * p + h : lane);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) x[k] = shfl2(x[k], src);
+      colv = shfl2(colv, src);
+      if (lane == 0) {
+        const int t = lperm[warp][p];
+        lperm[warp][p] = lperm[warp][q];
+        lperm[warp][q] = t;
+      }
+    }
+    const float2 piv = shfl2(colv, 2 * p);
+    if (lane == 0) check_pivot(a, piv);
+    const float2 pinv = crcp(piv);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int c = 8 * h + k;
+      const float2 rv = shfl2(x[k], 2 * p + h);
+      const float2 mult = c == p ? pinv : cmul(rv, pinv);
+      const float2 base = c == p ? make_float2(0.f, 0.f) : x[k];
+      x[k] = r == p ? mult : csub(base, cmul(colv, mult));
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int c = 8 * h + k;
+    G[r][c < nI ? lperm[warp][c] : c] = x[k];
+  }
+  __syncwarp();
+  float2* top = ftop(a, n, b);
+  for_divmod(lane, 32, nI * f, nI, [&](int e, int c, int rr) {
+    top[e] = c < nI ? G[rr][c] : cmul(G[rr][ia[warp][c - nI]], av[warp][c - nI]);
+  });
+  if (nB == 0) return;
+  float2* bl = fbl(a, n, b);
+  float2* S = fsch(a, n, b);
+  for_divmod(lane, 32, nB * nI, nB, [&](int e, int c, int j) {
+    const float2 t = cmul(bv[warp][j], G[ib[warp][j]][c]);
+    bl[e] = make_float2(-t.x, -t.y);
+  });
+  for_divmod(lane, 32, nB * nB, nB, [&](int e, int j, int l) {
+    const float2 t = cmul(cmul(bv[warp][j], G[ib[warp][j]][ia[warp][l]]), av[warp][l]);
+    S[e] = make_float2(-t.x, -t.y);
+  });
+}
+
+// Other small fronts: one CTA of NT threads per (node, problem).  The front
+// lives in shared memory (row stride ld, a multiple of 4 >= f, entries
+// beyond f zero) and is swept in blocks P of up to BS pivots, each block in
+// three phases:
+//   A. warp 0: LU with partial (row) pivoting of F[P, P], Pm F[P, P] = L U,
+//      padded with the identity to BS x BS; meanwhile the other warps copy the
+//      old pivot columns F[r, P] (r outside P), transposed, to Ct.
+//   B. row panel (a thread per column c): Rt[:, c] = L^-1 Pm F[P, c], then
+//      F[P, c] = U^-1 Rt[:, c]; for c in P the right-hand side is the unit
+//      vector, which writes F[P, P]^-1.  Column panel (a thread per row r):
+//      Ct[:, r] = (F[r, P] U^-1)^T, then F[r, P] = -(Ct[:, r]^T L^-1) Pm.
+// Only F[P, P]^-1 enters the sweep operator, so pivoting inside a block
+// leaves the result unchanged and keeps small pivots of a near-resonant
+// block from growing the rounding.
+//   C. rank-|P| update F[r, c] -= Ct[:, r] . Rt[:, c] of the entries outside
+//      the pivot rows and columns, a 4 x 4 register tile per thread and step.
+// The pivot order is the same as a pivot-by-pivot Gauss-Jordan sweep, so the
+// result is the same sweep operator.  The update takes the LU split
+// (F_rP U^-1)(L^-1 F_Pc), the right-looking form: the product of the old
+// column with the finished row panel, F_rP (A_PP^-1 F_Pc), is the same
+// number mathematically but cancels an order of magnitude more rounding on
+// ill-conditioned pivot blocks.  Three barriers per pivot block.
+template <int NT, int BS>
+__global__ void __launch_bounds__(NT, 768 / NT) k_front(Args a, const int* __restrict__ list, int ld) {
+  static_assert(NT >= 64 && BS <= 32, "k_front shape");
+  constexpr int NW = NT / 32;
+  extern __shared__ __align__(16) float2 sm[];
+  float2* F = sm;             // [ld][ld]
+  float2* Ct = sm + ld * ld;  // [BS][ld]: pivot columns, transposed
+  float2* Rt = Ct + BS * ld;  // [BS][ld]: L^-1 times the pivot rows
+  __shared__ float2 LU[BS][BS + 1];
+  __shared__ float2 dinv[BS];
+  __shared__ int pv[BS];  // row k of Pm F[P, P] is row pv[k] of F[P, P]
   const Node n = a.nodes[list[blockIdx.x]];
   const int b = blockIdx.y;
-  const int f = n.nI + n.nB, nI = n.nI, nB = n.nB;
-  const int tid = threadIdx.x, nt = TR * TC;
-  for (int e = tid; e < f * f; e += nt) F[e] = make_float2(0.f, 0.f);
+  const int f = n.nI + n.nB, nI = n.nI;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  {
+    float4* F4 = reinterpret_cast<float4*>(F);
+    for (int e = tid; e < ld * ld / 2; e += NT) F4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   __syncthreads();
-  for (int q = tid; q < n.ndesc; q += nt) {
+  for (int q = tid; q < n.ndesc; q += NT) {
     const Desc d = a.desc[n.desc + q];
     const float2 v = coef(a.op, b, d.cell, d.dir);
-    float2& t = F[d.row * f + d.col];
+    float2& t = F[d.row * ld + d.col];
     t = cadd(t, v);
   }
   __syncthreads();
@@ -237,83 +412,187 @@ __global__ void __launch_bounds__(TR * TC) k_small(Args a, const int* __restrict
   for (int s = 0; s < 2; ++s) {
     const int ch = n.child[s];
     if (ch < 0) continue;
-    const Node c = a.nodes[ch];
+    const int cnB = a.nodes[ch].nB;
     const int* map = a.cmap + n.cmap[s];
-    const float2* S = fsch(a, c, b);
-    for (int e = tid; e < c.nB * c.nB; e += nt) {
-      const int r = e / c.nB, q = e - r * c.nB;
-      float2& t = F[map[r] * f + map[q]];
-      t = cadd(t, S[e]);
+    const float2* S = fsch(a, a.nodes[ch], b);
+    for (int r = warp; r < cnB; r += NW) {
+      float2* row = F + map[r] * ld;
+      const float2* src = S + (size_t)r * cnB;
+      for (int q = lane; q < cnB; q += 32) {
+        float2& t = row[map[q]];
+        t = cadd(t, src[q]);
+      }
     }
     __syncthreads();
   }
-  const int ty = tid / TC, tx = tid - (tid / TC) * TC;
-  float2 reg[R][Cn];
+  for (int k0 = 0; k0 < nI; k0 += BS) {
+    const int nb = min(BS, nI - k0);
+    auto inP = [&](int i) { return i >= k0 && i < k0 + nb; };
+    // ---- A
+    if (warp == 0) {
+      if (lane < BS) {
 #pragma unroll
-  for (int u = 0; u < R; ++u)
-#pragma unroll
-    for (int v = 0; v < Cn; ++v) {
-      const int r = ty + TR * u, c = tx + TC * v;
-      reg[u][v] = (r < f && c < f) ? F[r * f + c] : make_float2(0.f, 0.f);
-    }
-  for (int p = 0; p < nI; ++p) {
-    // the owner of (p, p) publishes 1/F_pp
-    if ((p % TR) == ty && (p % TC) == tx) {
-      float2 d = make_float2(0.f, 0.f);
-#pragma unroll
-      for (int u = 0; u < R; ++u)
-#pragma unroll
-        for (int v = 0; v < Cn; ++v)
-          if (ty + TR * u == p && tx + TC * v == p) d = reg[u][v];
-      check_pivot(a, d);
-      s_pinv = crcp(d);
-    }
-    __syncthreads();
-    const float2 pinv = s_pinv;
-#pragma unroll
-    for (int u = 0; u < R; ++u)
-#pragma unroll
-      for (int v = 0; v < Cn; ++v) {
-        const int r = ty + TR * u, c = tx + TC * v;
-        if (r == p && c != p && c < f) rowbuf[c] = cmul(reg[u][v], pinv);
-        if (c == p && r != p && r < f) colbuf[r] = reg[u][v];
+        for (int r = 0; r < BS; ++r)
+          LU[r][lane] = (r < nb && lane < nb) ? F[(k0 + r) * ld + k0 + lane]
+                                              : make_float2(r == lane ? 1.f : 0.f, 0.f);
+        pv[lane] = lane;
       }
-    __syncthreads();
+      __syncwarp();
+      for (int k = 0; k < BS; ++k) {
+        if (k < nb) {
+          // the largest |entry| of column k among rows k .. nb-1 (lowest row on ties)
+          float m = -1.f;
+          int q = k;
+          if (lane >= k && lane < nb) {
+            const float2 v = LU[lane][k];
+            m = v.x * v.x + v.y * v.y;
+            q = lane;
+          }
 #pragma unroll
-    for (int u = 0; u < R; ++u) {
-      const int r = ty + TR * u;
-      if (r >= f) continue;
-      const float2 cr = colbuf[r];
-#pragma unroll
-      for (int v = 0; v < Cn; ++v) {
-        const int c = tx + TC * v;
-        if (c >= f) continue;
-        if (r == p) {
-          reg[u][v] = (c == p) ? pinv : rowbuf[c];
-        } else if (c == p) {
-          const float2 t = cmul(cr, pinv);
-          reg[u][v] = make_float2(-t.x, -t.y);
-        } else {
-          const float2 rc = rowbuf[c];
-          reg[u][v].x -= cr.x * rc.x - cr.y * rc.y;
-          reg[u][v].y -= cr.x * rc.y + cr.y * rc.x;
+          for (int o = 16; o > 0; o >>= 1) {
+            const float m2 = __shfl_xor_sync(0xffffffffu, m, o);
+            const int q2 = __shfl_xor_sync(0xffffffffu, q, o);
+            if (m2 > m || (m2 == m && q2 < q)) {
+              m = m2;
+              q = q2;
+            }
+          }
+          if (q != k) {  // warp-uniform
+            if (lane < BS) {
+              const float2 t = LU[k][lane];
+              LU[k][lane] = LU[q][lane];
+              LU[q][lane] = t;
+            }
+            if (lane == 0) {
+              const int t = pv[k];
+              pv[k] = pv[q];
+              pv[q] = t;
+            }
+          }
+          __syncwarp();
         }
+        const float2 piv = LU[k][k];
+        if (k < nb && lane == 0) check_pivot(a, piv);
+        const float2 pinv = crcp(piv);
+        if (lane > k && lane < BS) LU[lane][k] = cmul(LU[lane][k], pinv);
+        __syncwarp();
+        if (lane > k && lane < BS) {
+          const float2 ukj = LU[k][lane];
+#pragma unroll
+          for (int r = 1; r < BS; ++r)
+            if (r > k) LU[r][lane] = csub(LU[r][lane], cmul(LU[r][k], ukj));
+        }
+        __syncwarp();
+      }
+      if (lane < BS) dinv[lane] = crcp(LU[lane][lane]);
+    } else {
+      for (int k = warp - 1; k < BS; k += NW - 1)
+        for (int r = lane; r < ld; r += 32)
+          Ct[k * ld + r] = (k < nb && r < f && !inP(r)) ? F[r * ld + k0 + k] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    // ---- B (NT / 2 >= ld threads per panel)
+    if (tid < NT / 2) {
+      const int c = tid;
+      if (c < f) {
+        const bool piv = inP(c);
+        float2 x[BS];
+#pragma unroll
+        for (int r = 0; r < BS; ++r)
+          x[r] = piv ? make_float2(pv[r] == c - k0 ? 1.f : 0.f, 0.f)
+                     : (r < nb ? F[(k0 + pv[r]) * ld + c] : make_float2(0.f, 0.f));
+#pragma unroll
+        for (int r = 1; r < BS; ++r)
+#pragma unroll
+          for (int k = 0; k < r; ++k) x[r] = csub(x[r], cmul(LU[r][k], x[k]));
+#pragma unroll
+        for (int r = 0; r < BS; ++r) Rt[r * ld + c] = x[r];
+#pragma unroll
+        for (int r = BS - 1; r >= 0; --r) {
+#pragma unroll
+          for (int k = r + 1; k < BS; ++k) x[r] = csub(x[r], cmul(LU[r][k], x[k]));
+          x[r] = cmul(x[r], dinv[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < BS; ++r)
+          if (r < nb) F[(k0 + r) * ld + c] = x[r];
+      } else if (c < ld) {
+#pragma unroll
+        for (int r = 0; r < BS; ++r) Rt[r * ld + c] = make_float2(0.f, 0.f);
+      }
+    } else {
+      const int r = tid - NT / 2;
+      if (r < f && !inP(r)) {
+        float2 x[BS];
+#pragma unroll
+        for (int k = 0; k < BS; ++k) x[k] = Ct[k * ld + r];
+        // x U = a (left to right), then x L = y (right to left)
+#pragma unroll
+        for (int j = 0; j < BS; ++j) {
+#pragma unroll
+          for (int k = 0; k < j; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
+          x[j] = cmul(x[j], dinv[j]);
+        }
+#pragma unroll
+        for (int k = 0; k < BS; ++k) Ct[k * ld + r] = x[k];
+#pragma unroll
+        for (int j = BS - 2; j >= 0; --j)
+#pragma unroll
+          for (int k = j + 1; k < BS; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
+#pragma unroll
+        for (int k = 0; k < BS; ++k)
+          if (k < nb) F[r * ld + k0 + pv[k]] = make_float2(-x[k].x, -x[k].y);
       }
     }
-  }
-  float2* top = ftop(a, n, b);
-  float2* bl = fbl(a, n, b);
-  float2* S = fsch(a, n, b);
+    __syncthreads();
+    // ---- C
+    {
+      const int tcn = ld >> 2;
+      for_divmod(tid, NT, tcn * tcn, tcn, [&](int, int tr, int tc) {
+        const int R0 = tr * 4, C0 = tc * 4;
+        if ((R0 >= k0 && R0 + 4 <= k0 + nb) || (C0 >= k0 && C0 + 4 <= k0 + nb)) return;
+        float2 acc[4][4];
 #pragma unroll
-  for (int u = 0; u < R; ++u)
+        for (int i = 0; i < 4; ++i) {
+          const float4 u = *reinterpret_cast<const float4*>(F + (R0 + i) * ld + C0);
+          const float4 w = *reinterpret_cast<const float4*>(F + (R0 + i) * ld + C0 + 2);
+          acc[i][0] = make_float2(u.x, u.y);
+          acc[i][1] = make_float2(u.z, u.w);
+          acc[i][2] = make_float2(w.x, w.y);
+          acc[i][3] = make_float2(w.z, w.w);
+        }
+#pragma unroll 4
+        for (int k = 0; k < nb; ++k) {
+          const float4 c01 = *reinterpret_cast<const float4*>(Ct + k * ld + R0);
+          const float4 c23 = *reinterpret_cast<const float4*>(Ct + k * ld + R0 + 2);
+          const float4 r01 = *reinterpret_cast<const float4*>(Rt + k * ld + C0);
+          const float4 r23 = *reinterpret_cast<const float4*>(Rt + k * ld + C0 + 2);
+          const float2 cv[4] = {make_float2(c01.x, c01.y), make_float2(c01.z, c01.w),
+                                make_float2(c23.x, c23.y), make_float2(c23.z, c23.w)};
+          const float2 rv[4] = {make_float2(r01.x, r01.y), make_float2(r01.z, r01.w),
+                                make_float2(r23.x, r23.y), make_float2(r23.z, r23.w)};
 #pragma unroll
-    for (int v = 0; v < Cn; ++v) {
-      const int r = ty + TR * u, c = tx + TC * v;
-      if (r >= f || c >= f) continue;
-      if (r < nI) top[(size_t)c * nI + r] = reg[u][v];                  // column-major [G | H]
-      else if (c < nI) bl[(size_t)c * nB + (r - nI)] = reg[u][v];       // column-major -K
-      else S[(size_t)(r - nI) * nB + (c - nI)] = reg[u][v];
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              acc[i][j].x = fmaf(-cv[i].x, rv[j].x, acc[i][j].x);
+              acc[i][j].x = fmaf(cv[i].y, rv[j].y, acc[i][j].x);
+              acc[i][j].y = fmaf(-cv[i].x, rv[j].y, acc[i][j].y);
+              acc[i][j].y = fmaf(-cv[i].y, rv[j].x, acc[i][j].y);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          if (inP(R0 + i)) continue;
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (!inP(C0 + j)) F[(R0 + i) * ld + C0 + j] = acc[i][j];
+        }
+      });
     }
+    __syncthreads();
+  }
+  store_small(a, n, b, F, ld, tid, NT);
 }
 
 // ============================================================ large fronts
@@ -345,10 +624,6 @@ __global__ void k_extend(Args a, const int2* __restrict__ work, int slot) {
     float2* t = fel(a, n, b, pr, map[q]);
     *t = cadd(*t, S[q]);
   }
-}
-
-__device__ __forceinline__ float2 shfl2(float2 v, int src) {
-  return make_float2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
 // Pivot block of a block step, one warp per (large front, problem): the LU
@@ -818,11 +1093,12 @@ static void build_tree(std::vector<HNode>& nodes, int nx, int ny, int x0, int x1
 
 struct Level {
   std::vector<int> small, large;            // node ids
+  std::vector<int> leaf, front;             // small fronts: leaves (k_leaf), the rest (k_front)
   std::vector<int2> ext[2], panel, tiles;   // large-front work lists
   std::vector<int2> gemv, bwd;              // large-front apply work lists
-  int max_f_small = 0, max_f_large = 0, max_nI_large = 0;
+  int max_f_small = 0, max_nI_small = 0, max_f_large = 0, max_nI_large = 0;
   long long fac_lo = 0, fac_len = 0, s_len = 0;  // per-problem ranges of this depth
-  int *d_small = nullptr, *d_large = nullptr;
+  int *d_small = nullptr, *d_large = nullptr, *d_leaf = nullptr, *d_front = nullptr;
   int2 *d_ext[2] = {nullptr, nullptr}, *d_panel = nullptr, *d_tiles = nullptr;
   int2 *d_gemv = nullptr, *d_bwd = nullptr;
 };
@@ -843,7 +1119,8 @@ struct Shape {
   ~Shape() {
     if (device < 0) return;  // host-only analysis: nothing on a device
     for (auto& L : levels) {
-      cudaFree(L.d_small); cudaFree(L.d_large); cudaFree(L.d_ext[0]); cudaFree(L.d_ext[1]);
+      cudaFree(L.d_small); cudaFree(L.d_large); cudaFree(L.d_leaf); cudaFree(L.d_front);
+      cudaFree(L.d_ext[0]); cudaFree(L.d_ext[1]);
       cudaFree(L.d_panel); cudaFree(L.d_tiles); cudaFree(L.d_gemv); cudaFree(L.d_bwd);
     }
     cudaFree(d_nodes); cudaFree(d_cells); cudaFree(d_cmap); cudaFree(d_desc);
@@ -857,6 +1134,24 @@ static int upload(T** dst, const std::vector<T>& v) {
   CEV_CUDA(cudaMalloc((void**)dst, sizeof(T) * v.size()));
   CEV_CUDA(cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
   return CEV_OK;
+}
+
+// A front k_leaf can sweep: no children, nI and nB <= 16, and each boundary
+// cell coupled to exactly one interior cell in each direction (one F_IB entry
+// in its column, one F_BI entry in its row) -- the leaves of the dissection.
+static bool is_leaf(const Node& n, const Desc* d) {
+  if (n.child[0] >= 0 || n.child[1] >= 0 || n.nI > 16 || n.nB > 16) return false;
+  int ib[16] = {0}, bi[16] = {0};
+  for (int q = 0; q < n.ndesc; ++q) {
+    if (d[q].row < n.nI && d[q].col >= n.nI) ++ib[d[q].col - n.nI];
+    if (d[q].row >= n.nI) {
+      if (d[q].col >= n.nI) return false;
+      ++bi[d[q].row - n.nI];
+    }
+  }
+  for (int j = 0; j < n.nB; ++j)
+    if (ib[j] != 1 || bi[j] != 1) return false;
+  return true;
 }
 
 // Builds the tree, offsets, descriptors, maps and work lists of an nx x ny
@@ -972,7 +1267,13 @@ static int analyse(Shape& h, int nx, int ny, bool to_device) {
       n.lidx = -1;
       if (n.small) {
         L.small.push_back(k);
-        L.max_f_small = std::max(L.max_f_small, f);
+        if (is_leaf(n, desc.data() + n.desc)) {
+          L.leaf.push_back(k);
+        } else {
+          L.front.push_back(k);
+          L.max_f_small = std::max(L.max_f_small, f);
+          L.max_nI_small = std::max(L.max_nI_small, n.nI);
+        }
         continue;
       }
       dn[k].lidx = (int)L.large.size();
@@ -992,6 +1293,7 @@ static int analyse(Shape& h, int nx, int ny, bool to_device) {
     if (!to_device) continue;
     int rc;
     if ((rc = upload(&L.d_small, L.small)) || (rc = upload(&L.d_large, L.large)) ||
+        (rc = upload(&L.d_leaf, L.leaf)) || (rc = upload(&L.d_front, L.front)) ||
         (rc = upload(&L.d_ext[0], L.ext[0])) || (rc = upload(&L.d_ext[1], L.ext[1])) ||
         (rc = upload(&L.d_panel, L.panel)) || (rc = upload(&L.d_tiles, L.tiles)) ||
         (rc = upload(&L.d_gemv, L.gemv)) || (rc = upload(&L.d_bwd, L.bwd)))
@@ -1076,14 +1378,21 @@ static Args make_args(const cev_nd_precond_s* h, const Op& op) {
   return a;
 }
 
-template <int FS, int TR, int TC>
-static int launch_small(const Args& a, const Level& L, int B, cudaStream_t s) {
-  const int bytes = (FS * FS + 2 * FS) * (int)sizeof(float2);
-  int rc = allow_dynamic_smem((const void*)k_small<FS, TR, TC>, bytes);
+template <int NT, int BS>
+static int launch_front(const Args& a, const Level& L, int ld, int B, cudaStream_t s) {
+  const int bytes = (ld * ld + 2 * BS * ld) * (int)sizeof(float2);
+  int rc = allow_dynamic_smem((const void*)k_front<NT, BS>, bytes);
   if (rc != CEV_OK) return rc;
-  k_small<FS, TR, TC><<<dim3((unsigned)L.small.size(), B), TR * TC, bytes, s>>>(a, L.d_small);
-  CEV_CHECK_LAUNCH("nd k_small");
+  k_front<NT, BS><<<dim3((unsigned)L.front.size(), B), NT, bytes, s>>>(a, L.d_front, ld);
+  CEV_CHECK_LAUNCH("nd k_front");
   return CEV_OK;
+}
+
+template <int NT>
+static int launch_front_bs(const Args& a, const Level& L, int ld, int B, cudaStream_t s) {
+  if (L.max_nI_small <= 4) return launch_front<NT, 4>(a, L, ld, B, s);
+  if (L.max_nI_small <= 8) return launch_front<NT, 8>(a, L, ld, B, s);
+  return launch_front<NT, 16>(a, L, ld, B, s);
 }
 
 static unsigned zero_grid(long long elems) {
@@ -1103,11 +1412,19 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
         k_zero<<<zero_grid(L.s_len * B), 256, 0, s>>>(h->sar[d & 1], S.sa_pp[d & 1], 0, L.s_len, B);
       CEV_CHECK_LAUNCH("nd zero");
     }
-    if (!L.small.empty()) {
+    if (!L.leaf.empty()) {
+      const unsigned nl = (unsigned)L.leaf.size();
+      k_leaf<<<dim3((nl + LEAF_WARPS - 1) / LEAF_WARPS, B), LEAF_WARPS * 32, 0, s>>>(a, L.d_leaf,
+                                                                                   (int)nl);
+      CEV_CHECK_LAUNCH("nd k_leaf");
+    }
+    if (!L.front.empty()) {
+      // row stride: a multiple of 4 (16-byte rows of 4 x 4 tiles); NT / 2 >= ld
+      const int ld = (L.max_f_small + 3) & ~3;
       int rc;
-      if (L.max_f_small <= 32) rc = launch_small<32, 8, 16>(a, L, B, s);
-      else if (L.max_f_small <= 64) rc = launch_small<64, 16, 16>(a, L, B, s);
-      else rc = launch_small<128, 16, 32>(a, L, B, s);
+      if (ld <= 32) rc = launch_front_bs<64>(a, L, ld, B, s);
+      else if (ld <= 64) rc = launch_front_bs<128>(a, L, ld, B, s);
+      else rc = launch_front_bs<256>(a, L, ld, B, s);
       if (rc != CEV_OK) return rc;
     }
     if (L.large.empty()) continue;
