@@ -40,7 +40,7 @@ BYTES_PER_CELL_UPDATE = 28  # read+write Hx, Hy, Dz + read 1/eps (float32)
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_tm_strip launch (the
 # whole 2000-step run) on this workload (ncu capture summarised in
 # profiles/fdtd_tm_400x400_strip_kernel.md)
-STRIP400_DRAM_BYTES_PER_LAUNCH = 4367616 + 614144
+STRIP400_DRAM_BYTES_PER_LAUNCH = 4358912 + 653824
 
 
 def _peaks():
@@ -505,7 +505,7 @@ def run_ours(args):
                          "frac": achieved / peak, "traffic": STRIP400_DRAM_BYTES_PER_LAUNCH,
                          "traffic_unit": "bytes per launch (the whole 2000-step run)",
                          "algorithmic_bytes_per_launch": N * BYTES_PER_CELL_UPDATE * steps_t,
-                         "kernel": "k_tm_strip<float,16,3,8,persistent>", "peak_kind": peak_kind,
+                         "kernel": "k_tm_strip<float,14,3,8,persistent>", "peak_kind": peak_kind,
                          "note": "algorithmic 28 B/cell-update; one cooperative launch keeps the "
                                  "400x400 state in registers across all 2000 steps and exchanges "
                                  "8-cell rings between tiles through L2 every 8 steps, so DRAM "

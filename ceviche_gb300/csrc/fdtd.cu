@@ -212,13 +212,14 @@ __global__ void k_te_h(TEArgs<R> a) {
   const R ce = (eyd - ey) - (exr - ex);
   const AxisCoef<R> cx = a.ax[i], cy = a.ay[j];
   const R ph = cx.pH * cy.pH;
-  const R m1 = (R(1) - cx.aH - cy.aH - cx.aH * cy.aH) * ph;
+  const R m1 = fma(-cx.aH, cy.aH, (R(1) - cx.aH) - cy.aH) * ph;
   const R m2 = -a.S * ph;
   const R m4 = R(-4) * cx.aH * cy.aH * ph;
   const R hz = a.hz[n];
   R ih = R(0);
   if (m4 != R(0)) { ih = a.ihz[n] + hz; a.ihz[n] = ih; }
-  a.hz[n] = m1 * hz + m2 * ce + m4 * ih;
+  // explicit fused multiply-adds: the time-blocked TE kernel rounds the same way
+  a.hz[n] = fma(m4, ih, fma(m2, ce, m1 * hz));
 }
 
 template <typename R>
@@ -235,8 +236,8 @@ __global__ void k_te_d(TEArgs<R> a) {
   R icx = R(0), icy = R(0);
   if (cx.aD != R(0)) { icx = a.ichx[n] + chx; a.ichx[n] = icx; }
   if (cy.aD != R(0)) { icy = a.ichy[n] + chy; a.ichy[n] = icy; }
-  R vx = cy.f1D * a.dx[n] + cy.f2D * (chx + R(2) * cx.aD * icx);
-  R vy = cx.f1D * a.dy[n] + cx.f2D * (chy + R(2) * cy.aD * icy);
+  R vx = fma(cy.f2D, fma(R(2) * cx.aD, icx, chx), cy.f1D * a.dx[n]);
+  R vy = fma(cx.f2D, fma(R(2) * cy.aD, icy, chy), cx.f1D * a.dy[n]);
   if (a.jx) vx += a.jx[n];
   if (a.jy) vy += a.jy[n];
   a.dx[n] = vx;
@@ -1391,7 +1392,8 @@ static int pick_persist(int nx, int ny) {
 struct StripCfg {
   int w, s, k;
 };
-constexpr StripCfg STRIP_CFGS[] = {{16, 3, 8}, {16, 2, 4}, {16, 3, 4}, {32, 2, 8}};
+constexpr StripCfg STRIP_CFGS[] = {{16, 3, 8}, {16, 2, 4}, {16, 3, 4}, {32, 2, 8},
+                                   {14, 3, 8}, {21, 2, 8}};
 constexpr int N_STRIP_CFGS = sizeof(STRIP_CFGS) / sizeof(STRIP_CFGS[0]);
 
 static TileCfg strip_tile(const StripCfg& c) {
@@ -1469,9 +1471,13 @@ static int pick_strip(int nx, int ny, int np) {
     forced = std::atoi(e) - 1;
   }
   if (np > STRIP_PROBE_MAX) return -1;
-  for (int v = 0; v < N_STRIP_CFGS; ++v) {
-    if (forced >= 0 && v != forced) continue;
-    if (forced < 0 && v != 0) continue;  // (16, 3, 8) by default
+  // by default (14, 3, 8), then (16, 3, 8): the smaller tile spreads a grid
+  // over more SMs (400 x 400: 144 tiles of 26 x 48 instead of 117 of 32 x 48)
+  const int order[] = {4, 0};
+  const int n_try = forced >= 0 ? 1 : 2;
+  for (int i = 0; i < n_try; ++i) {
+    const int v = forced >= 0 ? forced : order[i];
+    if (v < 0 || v >= N_STRIP_CFGS) return -1;
     const TileCfg c = strip_tile(STRIP_CFGS[v]);
     if (nx < c.ti + 2 * c.k || ny < c.tj + 2 * c.k) continue;
     const int tiles = ((nx + c.ti - 1) / c.ti) * ((ny + c.tj - 1) / c.tj);
@@ -1671,6 +1677,10 @@ struct TEBArgs {
   R* probe_out;  // [t][np]
 };
 
+// a * b rounded on its own (no contraction into a following add)
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
 template <typename R, int TI, int TJ, int K, int NT>
 struct TeTile {
   static constexpr int RI = TI + 2 * K, RJ = TJ + 2 * K, RN = RI * RJ;
@@ -1775,16 +1785,16 @@ __global__ void __launch_bounds__(NT, 1) k_te_tile(TEBArgs<R> a) {
         const R eyd = (r < RI - 1) ? sEy[q + RJ] : ey;
         const R ce = (eyd - ey) - (exr - ex);
         if (!pml) {
-          hz[k] = hz[k] - S * ce;
+          hz[k] = fma(-S, ce, hz[k]);
         } else {
           const R ax = xaH[r], ay = yaH[c];
           const R ph = xpH[r] * ypH[c];
-          const R m1 = (R(1) - ax - ay - ax * ay) * ph;
+          const R m1 = fma(-ax, ay, (R(1) - ax) - ay) * ph;
           const R m2 = -S * ph;
           const R m4 = R(-4) * ax * ay * ph;
           R v = R(0);
           if (m4 != R(0)) { ih[k] += hz[k]; v = ih[k]; }
-          hz[k] = m1 * hz[k] + m2 * ce + m4 * v;
+          hz[k] = fma(m4, v, fma(m2, ce, m1 * hz[k]));  // as k_te_h
         }
         sHz[q] = hz[k];
       }
@@ -1802,19 +1812,19 @@ __global__ void __launch_bounds__(NT, 1) k_te_tile(TEBArgs<R> a) {
         const R chy = -(hz[k] - hzu);
         R vx, vy;
         if (!pml) {
-          vx = dx[k] + S * chx;
-          vy = dy[k] + S * chy;
+          vx = fma(S, chx, dx[k]);
+          vy = fma(S, chy, dy[k]);
         } else {
           const R ax = xaD[r], ay = yaD[c];
           R wx = R(0), wy = R(0);
           if (ax != R(0)) { icx[k] += chx; wx = icx[k]; }
           if (ay != R(0)) { icy[k] += chy; wy = icy[k]; }
-          vx = yf1[c] * dx[k] + yf2[c] * (chx + R(2) * ax * wx);
-          vy = xf1[r] * dy[k] + xf2[r] * (chy + R(2) * ay * wy);
+          vx = fma(yf2[c], fma(R(2) * ax, wx, chx), yf1[c] * dx[k]);  // as k_te_d
+          vy = fma(xf2[r], fma(R(2) * ay, wy, chy), xf1[r] * dy[k]);
         }
-        if (srcmask & (1u << k)) {
-          vx += sWx[q] * amp;
-          vy += sWy[q] * amp;
+        if (srcmask & (1u << k)) {  // the product rounded, then added, as a dense J
+          vx += mul_rn(sWx[q], amp);
+          vy += mul_rn(sWy[q], amp);
         }
         dx[k] = vx;
         dy[k] = vy;

@@ -208,7 +208,7 @@ def test_every_persistent_configuration(cev, cfg, shape, steps, monkeypatch):
         assert _rel(_np(A.fields[k]), _np(B.fields[k])) < 1e-6
 
 
-@pytest.mark.parametrize("cfg", range(4))  # every entry of STRIP_CFGS in csrc/fdtd.cu
+@pytest.mark.parametrize("cfg", range(6))  # every entry of STRIP_CFGS in csrc/fdtd.cu
 @pytest.mark.parametrize("shape,steps", [((141, 133), 85), ((141, 133), 93), ((70, 70), 61)])
 def test_every_strip_configuration(cev, cfg, shape, steps, monkeypatch):
     """The register-strip runner (forced through CEV_FDTD_STRIP; state in
