@@ -73,7 +73,7 @@ struct Node {
   int par;           // Schur arena of this node's depth (depth & 1)
   int small;         // f <= SMALL_F
   int lidx;          // large fronts: index in its depth's list of large fronts
-  int pad;
+  int po;            // large fronts: panel-scratch offset (in NB-element rows) within its depth
   long long top;     // [G | H] (nI x f), offset within one problem's factor block
   long long bl;      // -K (nB x nI)
   long long s;       // S (nB x nB, row-major) within one problem's block of arena par
@@ -109,8 +109,12 @@ struct Args {
   float2* fv;
   int* fault;  // set when a pivot is zero or not finite
   float2* lub; // LU factors of the current pivot blocks [B][large fronts][NB][NB]
+  int* lpv;    // their row permutations [B][large fronts][NB]
+  float2* rb;  // L^-1 Pm F[P, :] of the current block, [B][ps_pp], NB x f per front
+  float2* cb;  // F[:, P] U^-1 of the current block, [B][ps_pp], f x NB per front
   size_t n;    // cells per problem
   long long fac_pp, sa_pp[2], fv_pp;  // per-problem strides
+  long long ps_pp;                    // per-problem stride of rb / cb
 };
 
 __device__ __forceinline__ float2 eps_at(const Op& o, int b, int i, int j) {
@@ -170,6 +174,15 @@ __device__ float2 coef(const Op& o, int b, int cell, int dir) {
 __device__ __forceinline__ float2 crcp(float2 d) {
   const float q = 1.0f / (d.x * d.x + d.y * d.y);
   return make_float2(d.x * q, -d.y * q);
+}
+
+// acc - c r in complex arithmetic, four FP32 FMAs in a fixed order.
+__device__ __forceinline__ float2 cfms(float2 c, float2 r, float2 acc) {
+  acc.x = fmaf(-c.x, r.x, acc.x);
+  acc.x = fmaf(c.y, r.y, acc.x);
+  acc.y = fmaf(-c.x, r.y, acc.y);
+  acc.y = fmaf(-c.y, r.x, acc.y);
+  return acc;
 }
 
 __device__ __forceinline__ void check_pivot(const Args& a, float2 d) {
@@ -574,12 +587,7 @@ __global__ void __launch_bounds__(NT, 768 / NT) k_front(Args a, const int* __res
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              acc[i][j].x = fmaf(-cv[i].x, rv[j].x, acc[i][j].x);
-              acc[i][j].x = fmaf(cv[i].y, rv[j].y, acc[i][j].x);
-              acc[i][j].y = fmaf(-cv[i].x, rv[j].y, acc[i][j].y);
-              acc[i][j].y = fmaf(-cv[i].y, rv[j].x, acc[i][j].y);
-            }
+            for (int j = 0; j < 4; ++j) acc[i][j] = cfms(cv[i], rv[j], acc[i][j]);
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -626,16 +634,40 @@ __global__ void k_extend(Args a, const int2* __restrict__ work, int slot) {
   }
 }
 
-// Pivot block of a block step, one warp per (large front, problem): the LU
-// factors (no pivoting) of A_pp = F[k0:k0+nb, k0:k0+nb], padded with the
-// identity to NB x NB, go to the scratch `lub` for the two panel kernels, and
-// the explicit inverse replaces A_pp in the front.  The panels are then
-// formed by triangular solves with these factors, not by products with the
-// explicit inverse: on Helmholtz fronts the explicit-inverse form loses about
-// two orders of magnitude of accuracy in complex64.
+// Block step of a large front over the pivots P = [k0, k0 + nb), nb <= NB,
+// in four launches:
+//   k_pivblock: LU with partial (row) pivoting, Pm A_pp = L U (padded with
+//     the identity to NB x NB), to the scratch `lub` / `lpv`, and
+//     A_pp^-1 = U^-1 L^-1 Pm over A_pp in the front;
+//   k_rowpanel: RB = L^-1 Pm F[P, c] (scratch) and F[P, c] = U^-1 RB for the
+//     columns outside P;
+//   k_colpanel: CB = F[r, P] U^-1 (scratch) and F[r, P] = -(CB L^-1) Pm for
+//     the rows outside P;
+//   k_update: F[r, c] -= CB[r, :] RB[:, c] outside the pivot rows and columns.
+// The update takes the LU split (F_rP U^-1)(L^-1 Pm F_Pc), the right-looking
+// form; the product of the old column with the finished row panel,
+// F_rP (A_pp^-1 F_Pc), is the same number but cancels more rounding on
+// ill-conditioned pivot blocks, and explicit-inverse panels lose about two
+// orders of magnitude on Helmholtz fronts in complex64.  Pivoting inside the
+// block leaves the sweep operator unchanged (only A_pp^-1 enters it).
+__device__ __forceinline__ float2* lub_of(const Args& a, const Node& n, int b, int count) {
+  return a.lub + ((size_t)b * count + n.lidx) * NB * NB;
+}
+__device__ __forceinline__ int* lpv_of(const Args& a, const Node& n, int b, int count) {
+  return a.lpv + ((size_t)b * count + n.lidx) * NB;
+}
+__device__ __forceinline__ float2* rb_of(const Args& a, const Node& n, int b) {  // [NB][f]
+  return a.rb + (size_t)b * a.ps_pp + (size_t)n.po * NB;
+}
+__device__ __forceinline__ float2* cb_of(const Args& a, const Node& n, int b) {  // [f][NB]
+  return a.cb + (size_t)b * a.ps_pp + (size_t)n.po * NB;
+}
+
+// One warp per (large front, problem).
 __global__ void __launch_bounds__(128) k_pivblock(Args a, const int* __restrict__ list, int count,
                                                   int k0) {
   __shared__ float2 blk[4][NB][NB + 1];
+  __shared__ int pvs[4][NB];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int item = blockIdx.x * 4 + warp;
   if (item >= count) return;
@@ -645,12 +677,43 @@ __global__ void __launch_bounds__(128) k_pivblock(Args a, const int* __restrict_
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
   float2* base = ftop(a, n, b);
   float2(*B)[NB + 1] = blk[warp];
+  int* pv = pvs[warp];
   for (int r = 0; r < NB; ++r)
     B[r][lane] = (r < nb && lane < nb) ? base[(size_t)(k0 + r) * f + k0 + lane]
                                        : make_float2(r == lane ? 1.f : 0.f, 0.f);
+  pv[lane] = lane;
   __syncwarp();
-  // LU without pivoting, lane j owns column j
+  // LU with partial pivoting, lane j owns column j
   for (int k = 0; k < NB; ++k) {
+    if (k < nb) {
+      float m = -1.f;
+      int q = k;
+      if (lane >= k && lane < nb) {
+        const float2 v = B[lane][k];
+        m = v.x * v.x + v.y * v.y;
+        q = lane;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float m2 = __shfl_xor_sync(0xffffffffu, m, o);
+        const int q2 = __shfl_xor_sync(0xffffffffu, q, o);
+        if (m2 > m || (m2 == m && q2 < q)) {
+          m = m2;
+          q = q2;
+        }
+      }
+      if (q != k) {  // warp-uniform
+        const float2 t = B[k][lane];
+        B[k][lane] = B[q][lane];
+        B[q][lane] = t;
+        if (lane == 0) {
+          const int ti = pv[k];
+          pv[k] = pv[q];
+          pv[q] = ti;
+        }
+      }
+      __syncwarp();
+    }
     const float2 piv = B[k][k];
     if (k < nb && lane == 0) check_pivot(a, piv);
     const float2 pinv = crcp(piv);
@@ -662,13 +725,14 @@ __global__ void __launch_bounds__(128) k_pivblock(Args a, const int* __restrict_
     }
     __syncwarp();
   }
-  float2* lu = a.lub + ((size_t)b * count + n.lidx) * NB * NB;
+  float2* lu = lub_of(a, n, b, count);
   for (int r = 0; r < NB; ++r) lu[r * NB + lane] = B[r][lane];
-  // column `lane` of A_pp^-1 = U^-1 L^-1 e_lane
+  lpv_of(a, n, b, count)[lane] = pv[lane];
+  // column `lane` of A_pp^-1 = U^-1 L^-1 Pm e_lane
   float2 y[NB];
 #pragma unroll
   for (int r = 0; r < NB; ++r) {
-    float2 t = make_float2(r == lane ? 1.f : 0.f, 0.f);
+    float2 t = make_float2(pv[r] == lane ? 1.f : 0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < r; ++k) t = csub(t, cmul(B[r][k], y[k]));
     y[r] = t;
@@ -686,32 +750,42 @@ __global__ void __launch_bounds__(128) k_pivblock(Args a, const int* __restrict_
       if (r < nb) base[(size_t)(k0 + r) * f + k0 + lane] = y[r];
 }
 
-// Pivot rows: F[p, c] = U^-1 L^-1 F[p, c] for the 64 columns of one chunk
-// outside the pivot block, one thread per column (work: node index, column chunk).
+// Pivot rows, one thread per column (work: node index, column chunk of TILE).
 __global__ void __launch_bounds__(TILE) k_rowpanel(Args a, const int2* __restrict__ work, int k0,
                                                    int count) {
   __shared__ float2 LU[NB][NB + 1];
   __shared__ float2 dinv[NB];
+  __shared__ int pv[NB];
   const int2 w = work[blockIdx.x];
   const Node n = a.nodes[w.x];
   if (k0 >= n.nI) return;
   const int b = blockIdx.y;
   const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
-  const float2* lu = a.lub + ((size_t)b * count + n.lidx) * NB * NB;
+  const float2* lu = lub_of(a, n, b, count);
   for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) LU[e / NB][e % NB] = lu[e];
+  if (threadIdx.x < NB) pv[threadIdx.x] = lpv_of(a, n, b, count)[threadIdx.x];
   __syncthreads();
   if (threadIdx.x < NB) dinv[threadIdx.x] = crcp(LU[threadIdx.x][threadIdx.x]);
   __syncthreads();
   const int c = w.y * TILE + threadIdx.x;
-  if (c >= f || (c >= k0 && c < k0 + nb)) return;
+  if (c >= f) return;
+  float2* rb = rb_of(a, n, b);
+  if (c >= k0 && c < k0 + nb) {  // the pivot block's columns carry nothing into the update
+#pragma unroll
+    for (int r = 0; r < NB; ++r) rb[(size_t)r * f + c] = make_float2(0.f, 0.f);
+    return;
+  }
   float2* base = ftop(a, n, b);
   float2 x[NB];
 #pragma unroll
-  for (int r = 0; r < NB; ++r) x[r] = r < nb ? base[(size_t)(k0 + r) * f + c] : make_float2(0.f, 0.f);
+  for (int r = 0; r < NB; ++r)
+    x[r] = r < nb ? base[(size_t)(k0 + pv[r]) * f + c] : make_float2(0.f, 0.f);
 #pragma unroll
   for (int r = 1; r < NB; ++r)
 #pragma unroll
     for (int k = 0; k < r; ++k) x[r] = csub(x[r], cmul(LU[r][k], x[k]));
+#pragma unroll
+  for (int r = 0; r < NB; ++r) rb[(size_t)r * f + c] = x[r];
 #pragma unroll
   for (int r = NB - 1; r >= 0; --r) {
 #pragma unroll
@@ -723,11 +797,70 @@ __global__ void __launch_bounds__(TILE) k_rowpanel(Args a, const int2* __restric
     if (r < nb) base[(size_t)(k0 + r) * f + c] = x[r];
 }
 
+// Pivot columns, one thread per row (work: node index, row chunk of TILE).
+__global__ void __launch_bounds__(TILE) k_colpanel(Args a, const int2* __restrict__ work, int k0,
+                                                   int count) {
+  __shared__ float2 LU[NB][NB + 1];
+  __shared__ float2 dinv[NB];
+  __shared__ int pv[NB];
+  __shared__ float2 P[TILE][NB + 1];
+  const int2 w = work[blockIdx.x];
+  const Node n = a.nodes[w.x];
+  if (k0 >= n.nI) return;
+  const int b = blockIdx.y;
+  const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
+  const int r0 = w.y * TILE;
+  const float2* lu = lub_of(a, n, b, count);
+  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) LU[e / NB][e % NB] = lu[e];
+  if (threadIdx.x < NB) pv[threadIdx.x] = lpv_of(a, n, b, count)[threadIdx.x];
+  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
+    const int i = e / NB, k = e - i * NB;
+    const int r = r0 + i;
+    P[i][k] = (r < f && k < nb) ? *fel(a, n, b, r, k0 + k) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  if (threadIdx.x < NB) dinv[threadIdx.x] = crcp(LU[threadIdx.x][threadIdx.x]);
+  __syncthreads();
+  float2* cb = cb_of(a, n, b);
+  const int i = threadIdx.x, r = r0 + i;
+  if (r < f && !(r >= k0 && r < k0 + nb)) {
+    float2 x[NB];
+#pragma unroll
+    for (int k = 0; k < NB; ++k) x[k] = P[i][k];
+    // x U = a (columns left to right): the update's left factor
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+#pragma unroll
+      for (int k = 0; k < j; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
+      x[j] = cmul(x[j], dinv[j]);
+    }
+#pragma unroll
+    for (int k = 0; k < NB; ++k) cb[(size_t)r * NB + k] = x[k];
+    // then x L = y (right to left); column k of the result belongs to pivot pv[k]
+#pragma unroll
+    for (int j = NB - 2; j >= 0; --j)
+#pragma unroll
+      for (int k = j + 1; k < NB; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
+#pragma unroll
+    for (int k = 0; k < NB; ++k) P[i][k] = make_float2(-x[k].x, -x[k].y);
+  } else if (r < f) {
+#pragma unroll
+    for (int k = 0; k < NB; ++k) cb[(size_t)r * NB + k] = make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
+    const int ii = e / NB, k = e - ii * NB;
+    const int rr = r0 + ii;
+    if (k >= nb || rr >= f || (rr >= k0 && rr < k0 + nb)) continue;
+    *fel(a, n, b, rr, k0 + pv[k]) = P[ii][k];
+  }
+}
+
 // Rank-nb update of every entry outside the pivot rows and columns:
-// F[r, c] -= F[r, p] R[p, c], one UT_R x UT_C tile per CTA (work: node, tile).
-// 256 threads, each an 8 x 4 block (rows ty + 16u, cols tx + 16v).  Each
-// accumulator starts from the entry's old value, loaded before the panels,
-// so the read-modify-write latency overlaps the panel loads.
+// F[r, c] -= CB[r, :] RB[:, c], one UT_R x UT_C tile per CTA (work: node,
+// tile).  256 threads, each an 8 x 4 block (rows ty + 16u, cols tx + 16v).
+// Each accumulator starts from the entry's old value, loaded before the
+// panels, so the read-modify-write latency overlaps the panel loads.
 constexpr int UT_R = 128, UT_C = 64;
 constexpr int UPD_SMEM = (UT_R * (NB + 1) + NB * UT_C) * (int)sizeof(float2);
 
@@ -767,21 +900,23 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
                                                                : make_float2(0.f, 0.f);
     }
   }
-  // column panel F[r0 + i, k0 + k] (rows may be I or B rows; k0 + k < nI)
+  // panels: CB rows r0 .. r0 + UT_R - 1, RB columns c0 .. c0 + UT_C - 1
   {
+    const float2* cb = cb_of(a, n, b);
     const int k = threadIdx.x & (NB - 1);
 #pragma unroll 4
     for (int i = threadIdx.x >> 5; i < UT_R; i += 8) {
       const int r = r0 + i;
-      Cp[i][k] = (r < f && k < nb) ? row_lo(r)[k0 + k] : make_float2(0.f, 0.f);
+      Cp[i][k] = (r < f && k < nb) ? cb[(size_t)r * NB + k] : make_float2(0.f, 0.f);
     }
   }
   {
+    const float2* rb = rb_of(a, n, b);
     const int j = threadIdx.x & (UT_C - 1);
     const int c = c0 + j;
 #pragma unroll 4
     for (int k = threadIdx.x >> 6; k < NB; k += 4)
-      Rp[k][j] = (k < nb && c < f) ? top[(size_t)(k0 + k) * f + c] : make_float2(0.f, 0.f);
+      Rp[k][j] = (k < nb && c < f) ? rb[(size_t)k * f + c] : make_float2(0.f, 0.f);
   }
   __syncthreads();
 #pragma unroll 4
@@ -794,12 +929,7 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
 #pragma unroll
     for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        acc[u][v].x = fmaf(-cv[u].x, rv[v].x, acc[u][v].x);
-        acc[u][v].x = fmaf(cv[u].y, rv[v].y, acc[u][v].x);
-        acc[u][v].y = fmaf(-cv[u].x, rv[v].y, acc[u][v].y);
-        acc[u][v].y = fmaf(-cv[u].y, rv[v].x, acc[u][v].y);
-      }
+      for (int v = 0; v < 4; ++v) acc[u][v] = cfms(cv[u], rv[v], acc[u][v]);
   }
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
@@ -813,57 +943,6 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
       if (c >= f || (c >= k0 && c < k0 + nb)) continue;
       (c < nI ? lo : hi)[c] = acc[u][v];
     }
-  }
-}
-
-// Pivot columns: F[r, p] = -F[r, p] U^-1 L^-1 for the 64 rows of one chunk
-// outside the pivot block, one thread per row (work: node index, row chunk).
-__global__ void __launch_bounds__(TILE) k_colpanel(Args a, const int2* __restrict__ work, int k0,
-                                                   int count) {
-  __shared__ float2 LU[NB][NB + 1];
-  __shared__ float2 dinv[NB];
-  __shared__ float2 P[TILE][NB + 1];
-  const int2 w = work[blockIdx.x];
-  const Node n = a.nodes[w.x];
-  if (k0 >= n.nI) return;
-  const int b = blockIdx.y;
-  const int nb = min(NB, n.nI - k0), f = n.nI + n.nB;
-  const int r0 = w.y * TILE;
-  const float2* lu = a.lub + ((size_t)b * count + n.lidx) * NB * NB;
-  for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) LU[e / NB][e % NB] = lu[e];
-  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
-    const int i = e / NB, k = e - i * NB;
-    const int r = r0 + i;
-    P[i][k] = (r < f && k < nb) ? *fel(a, n, b, r, k0 + k) : make_float2(0.f, 0.f);
-  }
-  __syncthreads();
-  if (threadIdx.x < NB) dinv[threadIdx.x] = crcp(LU[threadIdx.x][threadIdx.x]);
-  __syncthreads();
-  const int i = threadIdx.x, r = r0 + i;
-  if (r < f && !(r >= k0 && r < k0 + nb)) {
-    float2 x[NB];
-#pragma unroll
-    for (int k = 0; k < NB; ++k) x[k] = P[i][k];
-    // x U = a (columns left to right), then x L = y (right to left)
-#pragma unroll
-    for (int j = 0; j < NB; ++j) {
-#pragma unroll
-      for (int k = 0; k < j; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
-      x[j] = cmul(x[j], dinv[j]);
-    }
-#pragma unroll
-    for (int j = NB - 2; j >= 0; --j)
-#pragma unroll
-      for (int k = j + 1; k < NB; ++k) x[j] = csub(x[j], cmul(x[k], LU[k][j]));
-#pragma unroll
-    for (int k = 0; k < NB; ++k) P[i][k] = make_float2(-x[k].x, -x[k].y);
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < TILE * NB; e += blockDim.x) {
-    const int ii = e / NB, k = e - ii * NB;
-    const int rr = r0 + ii;
-    if (k >= nb || rr >= f || (rr >= k0 && rr < k0 + nb)) continue;
-    *fel(a, n, b, rr, k0 + k) = P[ii][k];
   }
 }
 
@@ -909,8 +988,41 @@ __device__ __forceinline__ void gather_front(const Args& a, const ApplyIO& io, c
   }
 }
 
-// Forward, small fronts: one warp per (front, problem); lane r computes
-// u[r] = f_B[r] + sum_k (-K)[r][k] f_I[k] from the column-major -K.
+// y[r] = sum_k M[k * rows + r] x[k] for r < rows (column-major M in global
+// memory, x in shared memory), one warp; returns y[r] in the lanes with
+// lane % 32 == r (32-row chunks, call per chunk).  With rows <= 16 the two
+// half-warps take alternate k and are added by a shuffle; each lane keeps 8
+// independent loads in flight.
+__device__ __forceinline__ float2 colmajor_gemv(const float2* __restrict__ M, const float2* x,
+                                                int rows, int cols, int r0, int lane) {
+  const int g = rows - r0 <= 16 ? 2 : 1;
+  const int r = r0 + (g == 2 ? (lane & 15) : lane);
+  const int k0 = g == 2 ? (lane >> 4) : 0;
+  float2 a0 = make_float2(0.f, 0.f), a1 = a0;
+  if (r < rows) {
+    int k = k0;
+    for (; k + 7 * g < cols; k += 8 * g) {
+      float2 t[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) t[j] = __ldg(M + (size_t)(k + j * g) * rows + r);
+#pragma unroll
+      for (int j = 0; j < 8; j += 2) {
+        a0 = cfma(t[j], x[k + j * g], a0);
+        a1 = cfma(t[j + 1], x[k + (j + 1) * g], a1);
+      }
+    }
+    for (; k < cols; k += g) a0 = cfma(__ldg(M + (size_t)k * rows + r), x[k], a0);
+  }
+  float2 acc = cadd(a0, a1);
+  if (g == 2) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 16);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 16);
+  }
+  return acc;
+}
+
+// Forward, small fronts: one warp per (front, problem):
+// u = f_B + (-K) f_I from the column-major -K.
 __global__ void __launch_bounds__(WPB * 32) k_fwd_small(Args a, ApplyIO io,
                                                         const int* __restrict__ list, int count) {
   __shared__ float2 buf[WPB][SMALL_F];
@@ -923,16 +1035,16 @@ __global__ void __launch_bounds__(WPB * 32) k_fwd_small(Args a, ApplyIO io,
   gather_front(a, io, n, b, fvs, lane, 32, true);
   const float2* K = fbl(a, n, b);
   float2* out = ffv(a, n, b);
-  for (int r = lane; r < n.nB; r += 32) {
-    float2 acc = fvs[n.nI + r];
-    for (int k = 0; k < n.nI; ++k) acc = cfma(K[(size_t)k * n.nB + r], fvs[k], acc);
-    out[n.nI + r] = acc;
+  for (int r0 = 0; r0 < n.nB; r0 += 32) {
+    const float2 acc = colmajor_gemv(K, fvs, n.nB, n.nI, r0, lane);
+    const int r = r0 + lane;
+    if (r < n.nB && (n.nB - r0 > 16 || lane < 16)) out[n.nI + r] = cadd(fvs[n.nI + r], acc);
   }
   for (int t = lane; t < n.nI; t += 32) out[t] = fvs[t];
 }
 
-// Backward, small fronts: one warp per (front, problem); lane r computes
-// x_I[r] = sum_k [G | H][r][k] w[k], w = [f_I ; -x_B], from the column-major factor.
+// Backward, small fronts: one warp per (front, problem):
+// x_I = [G | H] w, w = [f_I ; -x_B], from the column-major factor.
 __global__ void __launch_bounds__(WPB * 32) k_bwd_small(Args a, ApplyIO io,
                                                         const int* __restrict__ list, int count) {
   __shared__ float2 buf[WPB][SMALL_F];
@@ -956,10 +1068,10 @@ __global__ void __launch_bounds__(WPB * 32) k_bwd_small(Args a, ApplyIO io,
   }
   __syncwarp();
   const float2* T = ftop(a, n, b);
-  for (int r = lane; r < n.nI; r += 32) {
-    float2 acc = make_float2(0.f, 0.f);
-    for (int k = 0; k < f; ++k) acc = cfma(T[(size_t)k * n.nI + r], wv[k], acc);
-    z[cl[r]] = acc;
+  for (int r0 = 0; r0 < n.nI; r0 += 32) {
+    const float2 acc = colmajor_gemv(T, wv, n.nI, f, r0, lane);
+    const int r = r0 + lane;
+    if (r < n.nI && (n.nI - r0 > 16 || lane < 16)) z[cl[r]] = acc;
   }
 }
 
@@ -974,18 +1086,26 @@ __global__ void __launch_bounds__(256) k_fwd_large(Args a, ApplyIO io, const int
   for (int t = threadIdx.x; t < n.nI + n.nB; t += blockDim.x) out[t] = fvs[t];
 }
 
-// Row dot product of a warp: sum_k row[k] x[k], four independent partial sums.
+// Row dot product of a warp: sum_k row[k] x[k]; each lane keeps 8
+// independent loads in flight (four partial sums).
 __device__ __forceinline__ float2 warp_dot(const float2* __restrict__ row, const float2* x, int len,
                                            int lane) {
   float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0, a3 = a0;
   int k = lane;
-  for (; k + 96 < len; k += 128) {
-    a0 = cfma(row[k], x[k], a0);
-    a1 = cfma(row[k + 32], x[k + 32], a1);
-    a2 = cfma(row[k + 64], x[k + 64], a2);
-    a3 = cfma(row[k + 96], x[k + 96], a3);
+  for (; k + 224 < len; k += 256) {
+    float2 t[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) t[j] = __ldg(row + k + 32 * j);
+    a0 = cfma(t[0], x[k], a0);
+    a1 = cfma(t[1], x[k + 32], a1);
+    a2 = cfma(t[2], x[k + 64], a2);
+    a3 = cfma(t[3], x[k + 96], a3);
+    a0 = cfma(t[4], x[k + 128], a0);
+    a1 = cfma(t[5], x[k + 160], a1);
+    a2 = cfma(t[6], x[k + 192], a2);
+    a3 = cfma(t[7], x[k + 224], a3);
   }
-  for (; k < len; k += 32) a0 = cfma(row[k], x[k], a0);
+  for (; k < len; k += 32) a0 = cfma(__ldg(row + k), x[k], a0);
   float2 acc = cadd(cadd(a0, a1), cadd(a2, a3));
   acc.x = warp_sumf(acc.x);
   acc.y = warp_sumf(acc.y);
@@ -1113,6 +1233,7 @@ struct Shape {
   int* d_cmap = nullptr;
   Desc* d_desc = nullptr;
   long long fac_pp = 0, sa_pp[2] = {0, 0}, fv_pp = 0;
+  long long ps_pp = 0;  // panel scratch per problem: NB x (sum of f over a depth's large fronts)
   double cmacs_pp = 0;  // Gauss-Jordan complex multiply-adds per problem
   size_t n_nodes = 0, n_desc = 0;
   long long cover[2] = {0, 0};
@@ -1261,10 +1382,12 @@ static int analyse(Shape& h, int nx, int ny, bool to_device) {
   // work lists per depth
   for (int d = 0; d < h.ndepth; ++d) {
     Level& L = h.levels[d];
+    long long po = 0;
     for (int k : by_depth[d]) {
       Node& n = dn[k];
       const int f = n.nI + n.nB;
       n.lidx = -1;
+      n.po = 0;
       if (n.small) {
         L.small.push_back(k);
         if (is_leaf(n, desc.data() + n.desc)) {
@@ -1277,6 +1400,8 @@ static int analyse(Shape& h, int nx, int ny, bool to_device) {
         continue;
       }
       dn[k].lidx = (int)L.large.size();
+      dn[k].po = (int)po;
+      po += f;
       L.large.push_back(k);
       L.max_f_large = std::max(L.max_f_large, f);
       L.max_nI_large = std::max(L.max_nI_large, n.nI);
@@ -1290,6 +1415,7 @@ static int analyse(Shape& h, int nx, int ny, bool to_device) {
       for (int c = 0; c < (n.nB + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.gemv.push_back(make_int2(k, c));
       for (int c = 0; c < (n.nI + GEMV_ROWS - 1) / GEMV_ROWS; ++c) L.bwd.push_back(make_int2(k, c));
     }
+    h.ps_pp = std::max(h.ps_pp, po * NB);
     if (!to_device) continue;
     int rc;
     if ((rc = upload(&L.d_small, L.small)) || (rc = upload(&L.d_large, L.large)) ||
@@ -1345,10 +1471,14 @@ struct cev_nd_precond_s {
   float2* sar[2] = {nullptr, nullptr};
   float2* fv = nullptr;
   float2* lub = nullptr;  // pivot-block LU scratch (factorisation only)
+  int* lpv = nullptr;     // pivot-block permutations (factorisation only)
+  float2* rb = nullptr;   // panel scratch (factorisation only)
+  float2* cb = nullptr;
   int* fault = nullptr;
   const cev_fdfd_plan_s* plan = nullptr;
   ~cev_nd_precond_s() {
     cudaFree(fac); cudaFree(sar[0]); cudaFree(sar[1]); cudaFree(fv); cudaFree(lub);
+    cudaFree(lpv); cudaFree(rb); cudaFree(cb);
     cudaFree(fault);
   }
 };
@@ -1370,6 +1500,10 @@ static Args make_args(const cev_nd_precond_s* h, const Op& op) {
   a.fv = h->fv;
   a.fault = h->fault;
   a.lub = h->lub;
+  a.lpv = h->lpv;
+  a.rb = h->rb;
+  a.cb = h->cb;
+  a.ps_pp = S.ps_pp;
   a.n = h->n;
   a.fac_pp = S.fac_pp;
   a.sa_pp[0] = S.sa_pp[0];
@@ -1441,8 +1575,8 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
     for (int k0 = 0; k0 < L.max_nI_large; k0 += NB) {
       k_pivblock<<<dim3((nl + 3) / 4, B), 128, 0, s>>>(a, L.d_large, (int)nl, k0);
       k_rowpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
-      k_update<<<dim3((unsigned)L.tiles.size(), B), 256, UPD_SMEM, s>>>(a, L.d_tiles, k0);
       k_colpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
+      k_update<<<dim3((unsigned)L.tiles.size(), B), 256, UPD_SMEM, s>>>(a, L.d_tiles, k0);
     }
     CEV_CHECK_LAUNCH("nd sweep");
   }
@@ -1556,8 +1690,14 @@ int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double*
     return fail(rc);
   size_t max_large = 0;
   for (const auto& L : S.levels) max_large = std::max(max_large, L.large.size());
-  if ((rc = alloc(&h->lub, max_large * B * NB * NB)))
+  if ((rc = alloc(&h->lub, max_large * B * NB * NB)) || (rc = alloc(&h->rb, (size_t)S.ps_pp * B)) ||
+      (rc = alloc(&h->cb, (size_t)S.ps_pp * B)))
     return fail(rc);
+  if (max_large > 0 && cudaMalloc((void**)&h->lpv, sizeof(int) * max_large * B * NB) != cudaSuccess) {
+    cudaGetLastError();
+    set_error("direct preconditioner: cannot allocate its pivot scratch");
+    return fail(CEV_ERR_CUDA);
+  }
   if (cudaMalloc((void**)&h->fault, sizeof(int)) != cudaSuccess) {
     cudaGetLastError();
     set_error("direct preconditioner: cannot allocate its fault flag");
@@ -1582,7 +1722,12 @@ int cev_nd_precond_create(cev_nd_precond* out, cev_fdfd_plan plan, const double*
   cudaFree(h->sar[1]);
   h->sar[0] = h->sar[1] = nullptr;
   cudaFree(h->lub);
+  cudaFree(h->lpv);
+  cudaFree(h->rb);
+  cudaFree(h->cb);
   h->lub = nullptr;
+  h->lpv = nullptr;
+  h->rb = h->cb = nullptr;
   *out = h;
   return CEV_OK;
 }
