@@ -1,5 +1,6 @@
 // Shared device/host helpers for the ceviche GB300 Yee-stencil library.
 #pragma once
+#include <initializer_list>
 
 #include <cuda_runtime.h>
 
@@ -95,6 +96,13 @@ int sm_count();
 // device (set once per device and kernel; thread-safe), and with carveout >= 0
 // the preferred shared-memory carve-out in percent.
 int allow_dynamic_smem(const void* fn, int bytes, int carveout = -1);
+// Device memory from the current device's default stream-ordered pool, which
+// keeps up to 256 MB of freed blocks for reuse: objects created and destroyed
+// in a loop (an FDTD plan per design iteration) then allocate without a driver
+// call.  Free with dev_free_all.
+int dev_alloc(void** p, size_t bytes, cudaStream_t s);
+// Waits for the device (as cudaFree does) and returns dev_alloc blocks to the pool.
+void dev_free_all(std::initializer_list<void*> ps);
 
 inline unsigned ceil_div(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
 

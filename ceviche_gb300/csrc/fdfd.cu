@@ -59,6 +59,38 @@ int allow_dynamic_smem(const void* fn, int bytes, int carveout) {
   return CEV_OK;
 }
 
+int dev_alloc(void** p, size_t bytes, cudaStream_t s) {
+  static std::mutex mu;
+  static std::map<int, bool> pooled;
+  int dev = 0;
+  CEV_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pooled[dev]) {
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long keep = 256ull << 20;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+      cudaGetLastError();
+      pooled[dev] = true;
+    }
+  }
+  *p = nullptr;
+  CEV_CUDA(cudaMallocAsync(p, bytes, s));
+  return CEV_OK;
+}
+
+void dev_free_all(std::initializer_list<void*> ps) {
+  bool any = false;
+  for (void* q : ps) any |= q != nullptr;
+  if (!any) return;
+  cudaDeviceSynchronize();
+  for (void* q : ps)
+    if (q) cudaFreeAsync(q, 0);
+  cudaGetLastError();
+}
+
 // ------------------------------------------------------------ PML profiles
 // sig_w / s_value of ceviche/derivatives.py:209-216 (m = 3, lnR = -30)
 static zd s_value(double l, double dw, double omega) {

@@ -1516,7 +1516,8 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
   }
   if (!p->shadow) {
     CEV_REQUIRE(!p->borrowed, "borrowed FDTD plan without a shadow state");
-    CEV_CUDA(cudaMalloc(&p->shadow, 6 * N * sizeof(R)));
+    int rc = dev_alloc(&p->shadow, 6 * N * sizeof(R), s);
+    if (rc != CEV_OK) return rc;
   }
   R* sh = (R*)p->shadow;
   R* bufA[6] = {(R*)st->hx, (R*)st->hy, (R*)st->dz, (R*)st->icex, (R*)st->icey, (R*)st->idz};
@@ -1545,14 +1546,17 @@ int run_tm_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
     if (p->pcfg != key) {
       std::vector<int> nbr;
       if (persist_neighbours(p->nx, p->ny, c, nbr)) {
-        cudaFree(p->pnbr);
-        cudaFree(p->pflags);
+        dev_free_all({p->pnbr, p->pflags});
         p->pnbr = nullptr;
         p->pflags = nullptr;
         p->pcfg = -1;
-        CEV_CUDA(cudaMalloc(&p->pnbr, sizeof(int) * nbr.size()));
-        CEV_CUDA(cudaMemcpy(p->pnbr, nbr.data(), sizeof(int) * nbr.size(), cudaMemcpyHostToDevice));
-        CEV_CUDA(cudaMalloc(&p->pflags, sizeof(int) * FLAG_STRIDE * (gx * gy + 1)));
+        int rc = dev_alloc((void**)&p->pnbr, sizeof(int) * nbr.size(), s);
+        if (rc == CEV_OK)
+          rc = dev_alloc((void**)&p->pflags, sizeof(int) * FLAG_STRIDE * (gx * gy + 1), s);
+        if (rc != CEV_OK) return rc;
+        // pageable source: the copy is staged before the call returns
+        CEV_CUDA(cudaMemcpyAsync(p->pnbr, nbr.data(), sizeof(int) * nbr.size(),
+                                 cudaMemcpyHostToDevice, s));
         p->pcfg = key;
         p->ptiles = gx * gy;
       }
@@ -1840,6 +1844,8 @@ __global__ void __launch_bounds__(NT, 1) k_te_tile(TEBArgs<R> a) {
       if (r >= K && r < K + TI && c >= K && c < K + TJ)
         a.probe_out[(size_t)(a.t0 + st) * a.np + k] = sHz[r * RJ + c];
     }
+    // the next H phase writes sHz: every probe read must be done first
+    if (a.np > 0) __syncthreads();
   }
 #pragma unroll
   for (int k = 0; k < CPT; ++k) {
@@ -1904,7 +1910,8 @@ int run_te_impl(cev_fdtd_plan p, const cev_fdtd_state* st, int nsteps, const cev
   }
   if (!p->shadow) {
     CEV_REQUIRE(!p->borrowed, "borrowed FDTD plan without a shadow state");
-    CEV_CUDA(cudaMalloc(&p->shadow, 6 * N * sizeof(R)));
+    int rc = dev_alloc(&p->shadow, 6 * N * sizeof(R), s);
+    if (rc != CEV_OK) return rc;
   }
   R* sh = (R*)p->shadow;
   R* bufA[6] = {(R*)st->hz, (R*)st->dx, (R*)st->dy, (R*)st->ihz, (R*)st->ichx, (R*)st->ichy};
@@ -2049,10 +2056,12 @@ int cev_fdtd_plan_create(cev_fdtd_plan* out, int nx, int ny, double dL, int npml
   sigma_profile(nx, npml_x, p->dt, p->aHx, p->aDx);
   sigma_profile(ny, npml_y, p->dt, p->aHy, p->aDy);
   cudaError_t e = cudaSuccess;
+  int arc = CEV_OK;
   auto up = [&](void** dst, const void* src, size_t bytes) {
-    if (e != cudaSuccess) return;
-    e = cudaMalloc(dst, bytes);
-    if (e == cudaSuccess) e = cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess || arc != CEV_OK) return;
+    arc = dev_alloc(dst, bytes, s);
+    // pageable source: the copy is staged before the call returns
+    if (arc == CEV_OK) e = cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s);
   };
   if (precision == CEV_PREC_C128) {
     auto cx = axis_coefs<double>(p->aHx, p->aDx, p->S), cy = axis_coefs<double>(p->aHy, p->aDy, p->S);
@@ -2064,9 +2073,13 @@ int cev_fdtd_plan_create(cev_fdtd_plan* out, int nx, int ny, double dL, int npml
     up(&p->ay, cy.data(), cy.size() * sizeof(cy[0]));
   }
   const size_t N = p->n();
-  if (e == cudaSuccess) e = cudaMalloc(&p->iez, N * p->rs());
-  if (e == cudaSuccess) e = cudaMalloc(&p->iexx, N * p->rs());
-  if (e == cudaSuccess) e = cudaMalloc(&p->ieyy, N * p->rs());
+  if (arc == CEV_OK && e == cudaSuccess) arc = dev_alloc(&p->iez, N * p->rs(), s);
+  if (arc == CEV_OK && e == cudaSuccess) arc = dev_alloc(&p->iexx, N * p->rs(), s);
+  if (arc == CEV_OK && e == cudaSuccess) arc = dev_alloc(&p->ieyy, N * p->rs(), s);
+  if (arc != CEV_OK) {
+    cev_fdtd_plan_destroy(p);
+    return arc;
+  }
   if (e != cudaSuccess) {
     cev_fdtd_plan_destroy(p);
     return cuda_status(e, "cev_fdtd_plan_create");
@@ -2082,14 +2095,7 @@ int cev_fdtd_plan_create(cev_fdtd_plan* out, int nx, int ny, double dL, int npml
 
 int cev_fdtd_plan_destroy(cev_fdtd_plan p) {
   if (!p) return CEV_OK;
-  cudaFree(p->pnbr);
-  cudaFree(p->pflags);
-  cudaFree(p->ax);
-  cudaFree(p->ay);
-  cudaFree(p->iez);
-  cudaFree(p->iexx);
-  cudaFree(p->ieyy);
-  cudaFree(p->shadow);
+  dev_free_all({p->pnbr, p->pflags, p->ax, p->ay, p->iez, p->iexx, p->ieyy, p->shadow});
   delete p;
   return CEV_OK;
 }
