@@ -67,7 +67,7 @@ def build(verbose=False, force=False, extra=()):
     with cf.ThreadPoolExecutor(max_workers=min(8, max(1, len(jobs)))) as ex:
         list(ex.map(run, jobs))
     if jobs or force or not _newer(LIB, objs):
-        run([nv, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-lcublas"])
+        run([nv, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
     return LIB
 
 

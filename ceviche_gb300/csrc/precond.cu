@@ -7,29 +7,110 @@
 // the caller from cev_fdfd_axis_matrix).  A vector of the basis is the
 // row-major (nx, ny) grid R, i.e. the column-major (ny x nx) matrix R^T, so
 //   (M^-1 R)^T = Vy ((Vy^-1 R^T Vx^-T) ./ D^T) Vx^T
-// is four complex GEMMs (cuBLAS, strided-batched over the problems; plain
-// library GEMMs) around one scaling kernel that also applies the basis
-// vector's scale sc_j.  The factors and GEMMs are complex128: with PML the
-// 1D operators are far from normal (cond(V) ~ 1e6 for 20 PML cells on a
-// 200-cell axis), and complex64 factors leave the preconditioner with O(0.1)
-// errors.
-#include <cublas_v2.h>
-
+// is four complex GEMMs (k_zgemm, strided-batched over the problems) around
+// one scaling kernel that also applies the basis vector's scale sc_j.  The
+// factors and GEMMs are complex128: with PML the 1D operators are far from
+// normal (cond(V) ~ 1e6 for 20 PML cells on a 200-cell axis), and complex64
+// factors leave the preconditioner with O(0.1) errors.
 #include "krylov.hpp"
 
 struct cev_sep_precond_s {
   int nx = 0, ny = 0, batch = 0, transpose = 0;
   const double2 *vx = nullptr, *vxi = nullptr, *vy = nullptr, *vyi = nullptr, *dinv = nullptr;
-  cublasHandle_t blas = nullptr;
 };
 
 namespace cev {
 
-static int blas_status(cublasStatus_t st, const char* where) {
-  if (st == CUBLAS_STATUS_SUCCESS) return CEV_OK;
-  set_error("%s: cuBLAS status %d", where, (int)st);
-  return CEV_ERR_CUDA;
+// Batched complex128 GEMM, column-major: C_b = op(A_b) B_b, op(A) = A^T when
+// TA (m x n result, inner dimension k; leading dimensions and per-problem
+// strides as given).  A T x T output tile per CTA of (T/U)^2 threads, each a
+// U x U block, 16-deep k chunks staged in shared memory.  On GB300 the FP64
+// FMA pipe is the bound, so what matters is occupying every SM: 64 x 64 tiles
+// for large or batched products, 16 x 16 tiles when those would leave SMs idle
+// (a single 200 x 200 product has 16 tiles of 64 but 169 of 16).
+constexpr int ZG_K = 16;
+template <bool TA, int T, int U>
+__global__ void __launch_bounds__((T / U) * (T / U)) k_zgemm(
+    int m, int n, int k, const double2* __restrict__ A, int lda, long long sa,
+    const double2* __restrict__ B, int ldb, long long sb, double2* __restrict__ C, int ldc,
+    long long sc) {
+  constexpr int TP = T / U, NT = TP * TP;
+  __shared__ double2 As[ZG_K][T + 1];  // [l][i] = op(A)[i][l]
+  __shared__ double2 Bs[ZG_K][T + 1];  // [l][j] = B[l][j]
+  const int bz = blockIdx.z;
+  A += bz * sa;
+  B += bz * sb;
+  C += bz * sc;
+  const int i0 = blockIdx.x * T, j0 = blockIdx.y * T;
+  const int tx = threadIdx.x % TP, ty = threadIdx.x / TP;
+  double2 acc[U][U];
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+#pragma unroll
+    for (int v = 0; v < U; ++v) acc[u][v] = make_double2(0.0, 0.0);
+  for (int k0 = 0; k0 < k; k0 += ZG_K) {
+    for (int e = threadIdx.x; e < T * ZG_K; e += NT) {
+      // op(A): element (i, l) is A[l + i lda] (TA) or A[i + l lda]; read along the contiguous index
+      int i, l;
+      if (TA) {
+        i = e / ZG_K;
+        l = e - i * ZG_K;
+      } else {
+        l = e / T;
+        i = e - l * T;
+      }
+      const int gi = i0 + i, gl = k0 + l;
+      As[l][i] = (gi < m && gl < k) ? (TA ? A[gl + (size_t)gi * lda] : A[gi + (size_t)gl * lda])
+                                    : make_double2(0.0, 0.0);
+      const int j = e / ZG_K, lb = e - j * ZG_K;
+      const int gj = j0 + j, glb = k0 + lb;
+      Bs[lb][j] = (gj < n && glb < k) ? B[glb + (size_t)gj * ldb] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int l = 0; l < ZG_K; ++l) {
+      double2 a[U], bv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) a[u] = As[l][tx + TP * u];
+#pragma unroll
+      for (int v = 0; v < U; ++v) bv[v] = Bs[l][ty + TP * v];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int v = 0; v < U; ++v) {
+          acc[u][v].x = fma(a[u].x, bv[v].x, acc[u][v].x);
+          acc[u][v].x = fma(-a[u].y, bv[v].y, acc[u][v].x);
+          acc[u][v].y = fma(a[u].x, bv[v].y, acc[u][v].y);
+          acc[u][v].y = fma(a[u].y, bv[v].x, acc[u][v].y);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+#pragma unroll
+    for (int v = 0; v < U; ++v) {
+      const int gi = i0 + tx + TP * u, gj = j0 + ty + TP * v;
+      if (gi < m && gj < n) C[gi + (size_t)gj * ldc] = acc[u][v];
+    }
 }
+
+template <bool TA>
+static int zgemm(int m, int n, int k, const double2* A, int lda, long long sa, const double2* B,
+                 int ldb, long long sb, double2* C, int ldc, long long sc, int batch,
+                 cudaStream_t s) {
+  const long long big = (long long)((m + 63) / 64) * ((n + 63) / 64) * batch;
+  if (big >= 2LL * sm_count()) {
+    const dim3 g((m + 63) / 64, (n + 63) / 64, batch);
+    k_zgemm<TA, 64, 4><<<g, 256, 0, s>>>(m, n, k, A, lda, sa, B, ldb, sb, C, ldc, sc);
+  } else {
+    const dim3 g((m + 15) / 16, (n + 15) / 16, batch);
+    k_zgemm<TA, 16, 2><<<g, 64, 0, s>>>(m, n, k, A, lda, sa, B, ldb, sb, C, ldc, sc);
+  }
+  CEV_CHECK_LAUNCH("k_zgemm");
+  return CEV_OK;
+}
+
 
 size_t precond_workspace_size(const cev_fdfd_plan_s* p, const cev_solve_opts& o) {
   if (o.precond != CEV_PRECOND_SEPARABLE || !p) return 0;
@@ -131,38 +212,21 @@ int precond_apply(Precond& pc, const KCtx& c, int j, int m, const float2* v, flo
   const int nx = h.nx, ny = h.ny, B = h.batch;
   const size_t total = st.n * (size_t)B;
   const long long sn = (long long)st.n, sx = (long long)nx * nx, sy = (long long)ny * ny;
-  const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
-  int rc = blas_status(cublasSetStream(h.blas, s), "cublasSetStream");
-  if (rc != CEV_OK) return rc;
-  auto C = [](const double2* p) { return (const cuDoubleComplex*)p; };
-  auto W = [](double2* p) { return (cuDoubleComplex*)p; };
   const unsigned g = std::max(1u, std::min(ceil_div(total, 256), 8u * sm_count()));
   k_c64_to_c128<<<g, 256, 0, s>>>(v, st.t1, total);
   CEV_CHECK_LAUNCH("k_c64_to_c128");
   // t2 = Vy^-1 R^T   (row-major Vy^-1 read transposed)
-  rc = blas_status(cublasZgemmStridedBatched(h.blas, CUBLAS_OP_T, CUBLAS_OP_N, ny, nx, ny, &one,
-                                             C(h.vyi), ny, sy, C(st.t1), ny, sn, &zero, W(st.t2),
-                                             ny, sn, B),
-                   "gemm 1");
+  int rc = zgemm<true>(ny, nx, ny, h.vyi, ny, sy, st.t1, ny, sn, st.t2, ny, sn, B, s);
   if (rc != CEV_OK) return rc;
   // t1 = t2 Vx^-T   (row-major Vx^-1 read as column-major is Vx^-T)
-  rc = blas_status(cublasZgemmStridedBatched(h.blas, CUBLAS_OP_N, CUBLAS_OP_N, ny, nx, nx, &one,
-                                             C(st.t2), ny, sn, C(h.vxi), nx, sx, &zero, W(st.t1),
-                                             ny, sn, B),
-                   "gemm 2");
+  rc = zgemm<false>(ny, nx, nx, st.t2, ny, sn, h.vxi, nx, sx, st.t1, ny, sn, B, s);
   if (rc != CEV_OK) return rc;
   k_sep_scale<<<g, 256, 0, s>>>(st.t1, h.dinv, c.sc, j, m, st.n, B, st.t2);
   CEV_CHECK_LAUNCH("k_sep_scale");
   // t1 = Vy t2 ; t2 = t1 Vx^T ; z = complex64(t2)
-  rc = blas_status(cublasZgemmStridedBatched(h.blas, CUBLAS_OP_T, CUBLAS_OP_N, ny, nx, ny, &one,
-                                             C(h.vy), ny, sy, C(st.t2), ny, sn, &zero, W(st.t1),
-                                             ny, sn, B),
-                   "gemm 3");
+  rc = zgemm<true>(ny, nx, ny, h.vy, ny, sy, st.t2, ny, sn, st.t1, ny, sn, B, s);
   if (rc != CEV_OK) return rc;
-  rc = blas_status(cublasZgemmStridedBatched(h.blas, CUBLAS_OP_N, CUBLAS_OP_N, ny, nx, nx, &one,
-                                             C(st.t1), ny, sn, C(h.vx), nx, sx, &zero, W(st.t2),
-                                             ny, sn, B),
-                   "gemm 4");
+  rc = zgemm<false>(ny, nx, nx, st.t1, ny, sn, h.vx, nx, sx, st.t2, ny, sn, B, s);
   if (rc != CEV_OK) return rc;
   k_c128_to_c64<<<g, 256, 0, s>>>(st.t2, z, total);
   CEV_CHECK_LAUNCH("k_c128_to_c64");
@@ -192,19 +256,12 @@ int cev_sep_precond_create(cev_sep_precond* out, cev_fdfd_plan plan, int transpo
   h->vy = (const double2*)vy;
   h->vyi = (const double2*)vyi;
   h->dinv = (const double2*)dinv;
-  const cublasStatus_t st = cublasCreate(&h->blas);
-  if (st != CUBLAS_STATUS_SUCCESS) {
-    delete h;
-    set_error("cublasCreate: status %d", (int)st);
-    return CEV_ERR_CUDA;
-  }
   *out = h;
   return CEV_OK;
 }
 
 int cev_sep_precond_destroy(cev_sep_precond h) {
   if (!h) return CEV_OK;
-  if (h->blas) cublasDestroy(h->blas);
   delete h;
   return CEV_OK;
 }

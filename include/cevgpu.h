@@ -136,7 +136,7 @@ typedef struct {
  * (k2 = eps0 mu0 w^2 dL^2; Tx, Ty the plan's 1D stencil operators, see
  * cev_fdfd_axis_matrix).  With Tx = Vx Lx Vx^-1 and Ty = Vy Ly Vy^-1 its
  * inverse is (Vx (x) Vy) diag(1/d) (Vx^-1 (x) Vy^-1): four dense complex
- * GEMMs per application (cuBLAS, strided-batched over the problems) and one
+ * GEMMs per application (strided-batched over the problems) and one
  * scaling kernel.  Used as the right preconditioner of flexible GMRES; the
  * solve still converges on the true operator to the FP64 residual.
  * vx, vxi: complex128 [batch][nx][nx] (row-major Vx, Vx^-1); vy, vyi:
