@@ -391,14 +391,13 @@ def fdtd_te_numbers(steps=2000):
             "note": "36 B/cell-update algorithmic (Hz, Dx, Dy r+w, 1/eps_xx, 1/eps_yy r)"}
 
 
-def fdtd_scaled_numbers(steps=256):
-    """Builder addition: the TM runner on a 4096x4096 grid (config-2 generator
-    scaled by area), where the state (> 400 MB) does not fit in L2, so the
-    roofline fraction measures HBM bandwidth."""
+def fdtd_scaled_numbers(steps=256, n=4096):
+    """Builder addition: the TM runner on an n x n grid (config-2 generator
+    scaled by area; 4096^2 and 8192^2), where the state (> 400 MB) does not
+    fit in L2, so the roofline fraction measures HBM bandwidth."""
     import torch
     import ceviche_gb300 as cev
     from ceviche_gb300.workloads import config2
-    n = 4096
     p = config2(N=n, steps=steps)
     F = cev.fdtd(p["eps"], p["dL"], p["npml"], precision="float32")
     amps = p["amps"][:steps]
@@ -536,6 +535,10 @@ def run_ours(args):
                 line["fdtd_scaled"] = fdtd_scaled_numbers()
             except Exception as e:
                 line["fdtd_scaled"] = {"error": repr(e)}
+            try:
+                line["fdtd_scaled_8192"] = fdtd_scaled_numbers(steps=128, n=8192)
+            except Exception as e:
+                line["fdtd_scaled_8192"] = {"error": repr(e)}
             try:
                 # the metric's "learned vs plain" part on config 4 (a shorter
                 # training schedule than --configs: 64 problems, 3000 + 1500 steps)
