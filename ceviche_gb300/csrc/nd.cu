@@ -858,13 +858,14 @@ __global__ void __launch_bounds__(TILE) k_colpanel(Args a, const int2* __restric
 
 // Rank-nb update of every entry outside the pivot rows and columns:
 // F[r, c] -= CB[r, :] RB[:, c], one UT_R x UT_C tile per CTA (work: node,
-// tile).  256 threads, each an 8 x 4 block (rows ty + 16u, cols tx + 16v).
-// Each accumulator starts from the entry's old value, loaded before the
-// panels, so the read-modify-write latency overlaps the panel loads.
-constexpr int UT_R = 128, UT_C = 64;
+// tile).  128 threads, each an 8 x 4 block (rows ty + 8u, cols tx + 16v);
+// four CTAs per SM, so one CTA's loads overlap another's FMAs.  Each
+// accumulator starts from the entry's old value, loaded before the panels,
+// so the read-modify-write latency overlaps the panel loads.
+constexpr int UT_R = 64, UT_C = 64, UT_NT = 128;
 constexpr int UPD_SMEM = (UT_R * (NB + 1) + NB * UT_C) * (int)sizeof(float2);
 
-__global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restrict__ work, int k0) {
+__global__ void __launch_bounds__(UT_NT, 4) k_update(Args a, const int2* __restrict__ work, int k0) {
   extern __shared__ float2 usm[];
   float2(*Cp)[NB + 1] = (float2(*)[NB + 1])usm;                  // [UT_R][NB + 1]
   float2(*Rp)[UT_C] = (float2(*)[UT_C])(usm + UT_R * (NB + 1));  // [NB][UT_C]
@@ -876,7 +877,7 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
   const int nb = min(NB, nI - k0), f = nI + nB;
   const int tc = (f + UT_C - 1) / UT_C;
   const int r0 = (w.y / tc) * UT_R, c0 = (w.y % tc) * UT_C;
-  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;  // ty < 8
   float2* const top = ftop(a, n, b);
   float2* const bl = fbl(a, n, b);
   float2* const sch = fsch(a, n, b);
@@ -889,7 +890,7 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
   float2 acc[8][4];
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
-    const int r = r0 + ty + 16 * u;
+    const int r = r0 + ty + 8 * u;
     const bool rok = r < f && !(r >= k0 && r < k0 + nb);
     const float2* lo = row_lo(min(r, f - 1));
     const float2* hi = row_hi(min(r, f - 1));
@@ -905,7 +906,7 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
     const float2* cb = cb_of(a, n, b);
     const int k = threadIdx.x & (NB - 1);
 #pragma unroll 4
-    for (int i = threadIdx.x >> 5; i < UT_R; i += 8) {
+    for (int i = threadIdx.x >> 5; i < UT_R; i += UT_NT / 32) {
       const int r = r0 + i;
       Cp[i][k] = (r < f && k < nb) ? cb[(size_t)r * NB + k] : make_float2(0.f, 0.f);
     }
@@ -915,7 +916,7 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
     const int j = threadIdx.x & (UT_C - 1);
     const int c = c0 + j;
 #pragma unroll 4
-    for (int k = threadIdx.x >> 6; k < NB; k += 4)
+    for (int k = threadIdx.x >> 6; k < NB; k += UT_NT / 64)
       Rp[k][j] = (k < nb && c < f) ? rb[(size_t)k * f + c] : make_float2(0.f, 0.f);
   }
   __syncthreads();
@@ -923,7 +924,7 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
   for (int k = 0; k < NB; ++k) {
     float2 cv[8], rv[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) cv[u] = Cp[ty + 16 * u][k];
+    for (int u = 0; u < 8; ++u) cv[u] = Cp[ty + 8 * u][k];
 #pragma unroll
     for (int v = 0; v < 4; ++v) rv[v] = Rp[k][tx + 16 * v];
 #pragma unroll
@@ -933,7 +934,7 @@ __global__ void __launch_bounds__(256, 2) k_update(Args a, const int2* __restric
   }
 #pragma unroll
   for (int u = 0; u < 8; ++u) {
-    const int r = r0 + ty + 16 * u;
+    const int r = r0 + ty + 8 * u;
     if (r >= f || (r >= k0 && r < k0 + nb)) continue;
     float2* lo = row_lo(r);
     float2* hi = row_hi(r);
@@ -1576,7 +1577,7 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
       k_pivblock<<<dim3((nl + 3) / 4, B), 128, 0, s>>>(a, L.d_large, (int)nl, k0);
       k_rowpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
       k_colpanel<<<dim3((unsigned)L.panel.size(), B), TILE, 0, s>>>(a, L.d_panel, k0, (int)nl);
-      k_update<<<dim3((unsigned)L.tiles.size(), B), 256, UPD_SMEM, s>>>(a, L.d_tiles, k0);
+      k_update<<<dim3((unsigned)L.tiles.size(), B), UT_NT, UPD_SMEM, s>>>(a, L.d_tiles, k0);
     }
     CEV_CHECK_LAUNCH("nd sweep");
   }
