@@ -403,6 +403,12 @@ typedef struct cev_fdtd_plan_s* cev_fdtd_plan;
  * Replaces ceviche/fdtd.py:12-72 (construction, setters), 213-316 (dt,
  * sigmas, update coefficients).  precision: CEV_PREC_C64 -> float32 fields,
  * CEV_PREC_C128 -> float64 fields.  eps: DEVICE double [nx][ny].
+ * A plan's buffers (tables, 1/eps, the runners' shadow state and exchange
+ * flags) come from the device's default stream-ordered memory pool, which
+ * keeps up to 256 MB of freed blocks for reuse, so plans created and
+ * destroyed in a loop allocate without a driver call; they are allocated on
+ * `stream` and usable on it at once.  cev_fdtd_plan_destroy waits for the
+ * device before returning the buffers to the pool.
  */
 CEV_API int cev_fdtd_plan_create(cev_fdtd_plan* plan, int nx, int ny, double dL, int npml_x, int npml_y,
                          int precision, const double* eps, cudaStream_t stream);
