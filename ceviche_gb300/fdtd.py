@@ -119,10 +119,12 @@ class fdtd:
     def initialize_fields(self):
         """Zero fields and PML integrals (fdtd.py:147-211)."""
         self.t_index = 0
-        z = lambda: torch.zeros((self.Nx, self.Ny), dtype=self.dtype, device="cuda")
-        self._st = {k: z() for k in _TM}
+        # one zeroed block (one allocation, one fill) holds the TM state and
+        # the zero field every key starts from
+        z = torch.zeros((len(_TM) + 1, self.Nx, self.Ny), dtype=self.dtype, device="cuda")
+        self._st = {k: z[i] for i, k in enumerate(_TM)}
         self._te = None
-        zero3 = torch.zeros((self.Nx, self.Ny, 1), dtype=self.dtype, device="cuda")
+        zero3 = z[len(_TM)].view(self.Nx, self.Ny, 1)
         self.fields = {k: zero3 for k in ("Ex", "Ey", "Ez", "Dx", "Dy", "Dz", "Hx", "Hy", "Hz")}
 
     def _iez(self):
@@ -223,9 +225,16 @@ class fdtd:
             a = a.detach().to("cuda", self.dtype).reshape(-1).contiguous()
             if a.numel() < steps:
                 raise ValueError(f"amps has {a.numel()} entries, need {steps}")
-            idx_d = idx.to("cuda", torch.int32).contiguous()
-            w_d = w.to("cuda", self.dtype).contiguous()
-            keep += [idx_d, w_d, a]
+            # cell indices and weights travel in one host-to-device copy: the
+            # weights first (8- or 4-byte aligned), then the int32 indices
+            ns, wb = int(idx.numel()), torch.finfo(self.dtype).bits // 8
+            host = torch.empty(ns * (wb + 4), dtype=torch.uint8)
+            host[: ns * wb] = w.to(self.dtype).view(torch.uint8)
+            host[ns * wb:] = idx.to(torch.int32).view(torch.uint8)
+            dev = host.to("cuda")
+            w_d = dev[: ns * wb].view(self.dtype)
+            idx_d = dev[ns * wb:].view(torch.int32)
+            keep += [dev, a]
             io.n_src = int(idx.numel())
             io.src_idx, io.src_w, io.amps = idx_d.data_ptr(), w_d.data_ptr(), a.data_ptr()
         out = None
