@@ -1559,6 +1559,9 @@ static int factor(cev_nd_precond_s* h, const Op& op, cudaStream_t s) {
       int rc;
       if (ld <= 32) rc = launch_front_bs<64>(a, L, ld, B, s);
       else if (ld <= 64) rc = launch_front_bs<128>(a, L, ld, B, s);
+      // fronts near 128: 8-pivot blocks keep the front plus its two panels
+      // under half of an SM's shared memory, so two CTAs share an SM
+      else if (ld > 96 && L.max_nI_small > 8) rc = launch_front<256, 8>(a, L, ld, B, s);
       else rc = launch_front_bs<256>(a, L, ld, B, s);
       if (rc != CEV_OK) return rc;
     }
