@@ -31,15 +31,17 @@
 // problems is one contiguous range.  Schur complements live in two arenas
 // alternating by depth parity (a node's children are one depth deeper).
 //
-// Kernels.  Fronts with f <= 128 (the lower levels, most nodes) are assembled
+// Kernels.  The leaves (4 x 4 boxes) need only the inverse of their 16 x 16
+// interior block, one warp each.  Other fronts with f <= 128 are assembled
 // and swept entirely in shared memory, one CTA per (node, problem), in blocks
-// of up to 16 pivots (LU of the pivot block, triangular-solve panels, a
-// register-tiled rank-16 update).  Larger fronts are assembled in
-// global memory and swept in blocks of NB = 32 pivots: invert the pivot block,
-// scale the pivot rows, a rank-32 update of every other entry (64 x 64 tiles,
-// FP32 FMA), and scale the pivot columns; the rank-32 update carries the
-// flops.  The apply kernels are bandwidth-bound GEMVs over the factor (warp
-// per row, coalesced along the rows).
+// of up to 16 pivots (pivoted LU of the pivot block, triangular-solve panels,
+// a register-tiled rank-16 update).  Larger fronts are assembled in global
+// memory and swept in blocks of NB = 32 pivots: pivoted LU of the pivot
+// block, row and column panels by triangular solves, then a rank-32 update of
+// every other entry (64 x 64 tiles, FP32 FMA) that carries the flops.  Every
+// update takes the right-looking LU split (F_rP U^-1)(L^-1 Pm F_Pc).  The
+// apply kernels are bandwidth-bound GEMVs over the factor (a warp per small
+// front, a warp per row of a large one).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
