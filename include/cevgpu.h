@@ -156,8 +156,11 @@ CEV_API int cev_sep_precond_destroy(cev_sep_precond h);
  * Direct preconditioner (CEV_PRECOND_DIRECT): a nested-dissection multifrontal
  * factorisation of the plan's non-dimensional operator A' (or A'^T with
  * transpose = 1) for eps (double [1 or batch][nx][ny], real or, with
- * cev_fdfd_plan_set_eps_complex, complex), in complex64 without pivoting and
- * without the periodic wrap entries.  It stands where ceviche factors the
+ * cev_fdfd_plan_set_eps_complex, complex), in complex64 and without the
+ * periodic wrap entries; the separators are eliminated in their dissection
+ * order, with partial pivoting only inside each block of up to 32 pivots
+ * (which leaves the factorisation's sparsity unchanged).  It stands where
+ * ceviche factors the
  * assembled matrix with SuperLU (ceviche/solvers.py:50-62, reached from
  * primitives.py:103-119); here the factors precondition flexible GMRES and the
  * FP64 true residual still decides convergence, so the complex64 rounding and
@@ -168,7 +171,8 @@ CEV_API int cev_sep_precond_destroy(cev_sep_precond h);
  * CEV_PRECOND_SHIFTED_LAPLACIAN uses.  The handle owns its factors (about
  * 80-110 complex64 numbers per cell and problem; cev_nd_precond_info) and
  * keeps a pointer to the plan, which must outlive it.  create synchronises
- * the stream; it returns CEV_ERR_NUMERIC for a zero pivot.
+ * the stream; it returns CEV_ERR_NUMERIC for a zero or non-finite pivot
+ * (a pivot block that is singular even with pivoting).
  * apply: z = M^-1 v for every problem (complex64 [batch][nx][ny]).
  */
 typedef struct cev_nd_precond_s* cev_nd_precond;
